@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 span mesher: MeshBuffer::generate_for_box on one
+octree span of 512^3 cells (513^3 = 135,005,697 corners), Mandelbulb P=8,
+max_iters 15, bailout 2.5, over [-1.2, 1.2]^3 (widened by one cell per side,
+src/mesh/buffer.rs:64-67).  One step = one full mesh: distance estimator at
+every corner, surface-cell compaction, vertex placement with the reference's
+six-sample normals, and the quad index list.
+
+Prints one JSON line.  `value` = corners processed per second (whole job,
+all ranks) with outputs left in HBM, timed with CUDA events on the mesher's
+stream; `e2e` = the same through cg_generate_for_box into pinned host buffers
+(device-to-host copies inside the timed region).  `--impl reference` times
+the CPU restatement of the reference's mesher (the reference itself, Rust and
+x86-only, cannot be built here) on all host cores.
+"""
+import argparse
+import concurrent.futures as cf
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DE pts/s fwd & fwd+adjoint vs FD normals, 1 GB300, % FP32 peak"
+UNIT = "pts/s"
+RES = 512
+SHAPE = dict(power=8, max_iters=15, bailout=2.5)
+WORKLOAD = ("single octree span, 512^3 cells / 513^3 = 135,005,697 corners, Mandelbulb P=8 "
+            "max_iters 15 bailout 2.5, span [-1.2,1.2]^3; DE + surface cells + vertices with "
+            "FD normals + quad indices")
+FLOPS_PER_STEP = 76   # P=8 iteration: magnitude, dr, polynomial, + p (each op = 1 flop)
+FLOPS_PER_ESCAPE = 6  # the final magnitude of an escaping point
+FLOPS_PER_POINT = 4   # ln(r) * r, * 0.5, / dr
+LAUNCHES_PER_MESH = 13  # k_de_grid, k_sign_words, k_cells, 3x scan, k_vertex_list, k_place,
+#                         k_quad_count, 3x scan, k_quad_emit
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------- CPU side
+def leaf_spans(depth: int = 3):
+    """The octree leaves of [-1.2,1.2]^3 at `depth` (create_spans order)."""
+    from cantucci_gb300.api import Span, create_spans
+    level = [Span(*__import__("cantucci_gb300.workloads", fromlist=["x"]).SPAN_C1)]
+    for _ in range(depth):
+        level = [c for s in level for c in create_spans(s)]
+    return level
+
+
+def cpu_mesh_sample(stride: int = 4, threads: int = None):
+    """The reference's CPU path on a bounded sample of the same workload: the
+    512 depth-3 octree leaves of the span (res 64 each, the same cell size as
+    res 512 over the whole span), every `stride`-th leaf, one leaf per worker
+    thread as ShapeMesh's thread pool runs them (src/mesh/mod.rs:58-63,141).
+    Returns (corners/s, threads, corners, seconds, sample text)."""
+    import numpy as np
+    import oracle
+    threads = threads or (os.cpu_count() or 1)
+    leaves = leaf_spans(3)[::stride]
+    shape = oracle.mandelbulb(**SHAPE)
+    oracle.lib()
+
+    def one(sp):
+        span = np.concatenate([sp.start, sp.end]).astype(np.float32)
+        r = oracle.generate_for_box(shape, span, 64, nthreads=1, vcap=64 ** 3, icap=18 * 64 ** 3)
+        assert r["rc"] == 0
+        return 65 ** 3
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        pts = sum(ex.map(one, leaves))
+    dt = time.perf_counter() - t0
+    text = ("%d of the 512 depth-3 octree leaves of the span (every %dth), res 64 each (%d "
+            "corners), oracle C restatement of generate_for_box, one leaf per thread" %
+            (len(leaves), stride, pts))
+    return pts / dt, threads, pts, dt, text
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU mesher on all host cores, rank 0 only."""
+    if rank != 0:
+        return
+    stride = 4
+    for _ in range(args.warmup):
+        cpu_mesh_sample(stride)
+    rates, secs, pts, threads, text = [], 0.0, 0, 0, ""
+    for _ in range(args.steps):
+        r, threads, p, dt, text = cpu_mesh_sample(stride)
+        rates.append(r)
+        secs += dt
+        pts += p
+    value = pts / secs
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "res": RES},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": text + " (the Rust reference is x86-only and not buildable "
+                                          "here; this is its C restatement)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU side
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import _ffi, workloads as W
+
+    torch.cuda.set_device(local_rank)
+    lib = _ffi.load()
+    dev = local_rank
+    shape = cg.Mandelbulb(**SHAPE)
+    span = cg.Span(*W.SPAN_C1)
+    res = args.res
+    n_pts = (res + 1) ** 3
+    mesher = cg.Mesher(dev)
+    sp = C.c_void_p()
+    _ffi.check(lib.cg_mesher_stream(mesher.handle, C.byref(sp)))
+    stream = torch.cuda.ExternalStream(sp.value, device=dev)
+
+    # Size the outputs from a first (untimed) mesh.
+    vcap, icap = max(res ** 3 // 16, 4096), max(18 * res ** 3 // 16, 65536)
+    verts_d = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
+    idx_d = torch.empty(icap, dtype=torch.int32, device=dev)
+    nv, ni, _ = mesher.generate_device(span, shape, res, verts_d, idx_d)
+
+    def step_device():
+        return mesher.generate_device(span, shape, res, verts_d, idx_d)
+
+    for _ in range(args.warmup):
+        step_device()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dev)).split(",")[0])
+                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else dev)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    stage = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        _, _, tm = step_device()
+        stage.append((tm.first_ms, tm.second_ms, tm.third_ms))
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    t_local = ms * 1e-3
+    t_max = t_local
+    if world > 1:
+        t = torch.tensor([t_local], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * n_pts * args.steps / t_max
+
+    # End to end: the C ABI with host (pinned) output buffers.
+    verts_h = torch.empty((vcap, 7), dtype=torch.float32, pin_memory=True)
+    idx_h = torch.empty(icap, dtype=torch.int32, pin_memory=True)
+    verts_np = verts_h.numpy().view(cg.VERTEX_DTYPE).reshape(-1)
+    idx_np = idx_h.numpy().view(np.uint32)
+    mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np)
+    torch.cuda.synchronize(dev)
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np)
+    f1.record(stream)
+    f1.synchronize()
+    e2e_s = f0.elapsed_time(f1) * 1e-3
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * n_pts * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": C.sizeof(_ffi.CgSpan) + C.sizeof(_ffi.CgShape),
+           "d2h_bytes_per_step": nv * 28 + ni * 4 + 16,
+           "note": "inputs are the span and shape (kernel parameters); outputs are the mesh"}
+
+    # Roofline of the dominant kernel (k_de_grid): algorithmic flops from the
+    # rotate steps actually executed, over its CUDA-event time per launch.
+    steps_c, esc_c = C.c_uint64(), C.c_uint64()
+    _ffi.check(lib.cg_span_grid_work(C.byref(shape._cshape()), C.byref(span.to_c()), res,
+                                     C.byref(steps_c), C.byref(esc_c)))
+    flops = (FLOPS_PER_STEP * steps_c.value + FLOPS_PER_ESCAPE * esc_c.value +
+             FLOPS_PER_POINT * n_pts)
+    de_ms = statistics.mean(s[0] for s in stage)
+    achieved = flops / (de_ms * 1e-3) / 1e12
+    peak = C.c_double()
+    _ffi.check(lib.cg_fp32_peak_probe(20000, C.byref(peak)))
+    peak_tf = peak.value / 1e12
+    roofline = {
+        "bound": "fp32", "kernel": "k_de_grid", "achieved": achieved, "peak": peak_tf,
+        "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
+        "peak_source": "measured in this run: FFMA chains, 2 flop per FFMA (FP32 pipe peak; "
+                       "not in MEASURED_PEAKS.json)",
+        "algorithmic_flops_per_launch": flops,
+        "mean_steps_per_point": steps_c.value / n_pts,
+        "flop_model": "76 per P=8 iteration + 6 per escape + 4 per point (add/sub/mul/div/sqrt"
+                      " = 1 each, as the reference writes them; FMA never used)",
+        "ops_frac_of_issue_peak": 2.0 * achieved / peak_tf,
+        "ops_note": "each reference op is one FP32-pipe instruction (bit-exact => no FMA), so "
+                    "the pipe's op peak is half its FMA flop peak",
+    }
+    if args.traffic is not None:
+        roofline["traffic"] = args.traffic
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "res": res, "corners": n_pts,
+                   "l2": "no flush: each step's working set (1.1 GB grids) exceeds the 129 MB L2",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "numerics": "exact (bit-identical loop state to the reference)"},
+        "stages_ms": {"first": statistics.mean(s[0] for s in stage),
+                      "second": statistics.mean(s[1] for s in stage),
+                      "third": statistics.mean(s[2] for s in stage)},
+        "mesh": {"vertices": nv, "indices": ni},
+        "de_kernel_pts_per_s": n_pts / (de_ms * 1e-3),
+        "roofline": roofline, "e2e": e2e, "clocks": clk,
+        "gpu_launches": LAUNCHES_PER_MESH * args.steps,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r, threads, p, dt, text = cpu_mesh_sample(4)
+        line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": text, "seconds": dt}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    mesher.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--res", type=int, default=RES)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per k_de_grid launch from an ncu capture")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group("nccl")
+    import __graft_entry__
+    __graft_entry__.build()
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,11 @@
+"""GB300 (sm_103a) Mandelbulb distance estimation, span meshing and sphere
+tracing behind cantucci's Shape / MeshBuffer API.
+
+The compute lives in libcantucci_gpu.so (include/cantucci_gpu.h); this
+package is the host-side mirror of the reference's Rust interface.
+"""
+from ._ffi import CantucciError, VERTEX_DTYPE, load  # noqa: F401
+from .api import (Mandelbulb, MandelbulbPolar, MeshBuffer, Mesher, Shape, Span, Sphere,  # noqa: F401
+                  Timings, create_spans, march)
+
+__version__ = "0.1.0"

@@ -1,0 +1,105 @@
+"""ctypes binding of the C ABI in include/cantucci_gpu.h.
+
+The library is built in-tree (cantucci_gb300/_lib/libcantucci_gpu.so).
+There is no fallback: if it is missing or fails to load, every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libcantucci_gpu.so")
+
+CG_OK, CG_EINVAL, CG_ECAPACITY, CG_ELERP, CG_ECUDA, CG_ENOMEM, CG_ETIMEOUT, CG_ENODEV = range(8)
+STATUS_NAMES = {0: "CG_OK", 1: "CG_EINVAL", 2: "CG_ECAPACITY", 3: "CG_ELERP", 4: "CG_ECUDA",
+                5: "CG_ENOMEM", 6: "CG_ETIMEOUT", 7: "CG_ENODEV"}
+
+CG_SHAPE_MANDELBULB, CG_SHAPE_SPHERE, CG_SHAPE_MANDELBULB_POLAR = 0, 1, 2
+CG_NUMERICS_EXACT, CG_NUMERICS_FAST = 0, 1
+CG_NORMALS_FD, CG_NORMALS_ADJOINT = 0, 1
+
+
+class CgShape(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("power", C.c_int32),
+        ("power_f", C.c_float),
+        ("max_iters", C.c_uint32),
+        ("bailout", C.c_float),
+        ("rot", C.c_float * 3),
+        ("center", C.c_float * 3),
+        ("radius", C.c_float),
+    ]
+
+
+class CgSpan(C.Structure):
+    _fields_ = [("start", C.c_float * 3), ("end", C.c_float * 3)]
+
+
+class CgTimings(C.Structure):
+    _fields_ = [("first_ms", C.c_float), ("second_ms", C.c_float), ("third_ms", C.c_float),
+                ("vertices", C.c_uint32), ("faces", C.c_uint32)]
+
+
+VERTEX_DTYPE = np.dtype([("position", "<f4", (3,)), ("normal", "<f4", (3,)),
+                         ("distance_from_surface", "<f4")])
+
+# Every symbol include/cantucci_gpu.h declares: (name, restype, argtypes).
+_vp, _u32, _u64, _f32, _i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_int
+_shp, _spp, _tmp = C.POINTER(CgShape), C.POINTER(CgSpan), C.POINTER(CgTimings)
+SIGNATURES = [
+    ("cg_abi_version", _i32, []),
+    ("cg_last_error", C.c_char_p, []),
+    ("cg_sizeof_shape", _u32, []),
+    ("cg_sizeof_vertex", _u32, []),
+    ("cg_min_distance_from", _i32, [_shp, _vp, _u64, _vp, _u32, _vp]),
+    ("cg_contains", _i32, [_shp, _vp, _u64, _vp, _vp]),
+    ("cg_de_span_grid", _i32, [_shp, _spp, _u32, _vp, _u32, _vp]),
+    ("cg_mandelbulb_state", _i32, [_shp, _vp, _u64, _vp, _vp]),
+    ("cg_mesher_create", _i32, [_i32, C.POINTER(_vp)]),
+    ("cg_mesher_destroy", None, [_vp]),
+    ("cg_mesher_set_normals", _i32, [_vp, _u32]),
+    ("cg_generate_for_box", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
+                                   C.POINTER(_u64), C.POINTER(_u64), _tmp]),
+    ("cg_generate_for_box_device", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
+                                          C.POINTER(_u64), C.POINTER(_u64), _tmp]),
+    ("cg_mesher_dists", _i32, [_vp, C.POINTER(_vp), C.POINTER(_u32)]),
+    ("cg_mesher_points", _i32, [_vp, _vp]),
+    ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
+    ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),
+    ("cg_span_grid_work", _i32, [_shp, _spp, _u32, C.POINTER(_u64), C.POINTER(_u64)]),
+    ("cg_fp32_peak_probe", _i32, [_u32, C.POINTER(C.c_double)]),
+]
+
+_lib = None
+
+
+class CantucciError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def load():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libcantucci_gpu.so is not built; run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        if L.cg_sizeof_shape() != C.sizeof(CgShape) or L.cg_sizeof_vertex() != VERTEX_DTYPE.itemsize:
+            raise ImportError("cantucci_gpu ABI layout mismatch")
+        _lib = L
+    return _lib
+
+
+def check(status: int):
+    if status != CG_OK:
+        raise CantucciError(status, load().cg_last_error().decode(errors="replace"))
+    return status

@@ -1,0 +1,50 @@
+// common.cuh -- error plumbing and launch helpers shared by the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "cantucci_gpu.h"
+
+namespace cg {
+
+// Last error message of this host thread (cg_last_error()).
+void set_error(const char* fmt, ...);
+const char* get_error();
+
+inline cg_status cuda_status(cudaError_t e, const char* what, const char* file, int line) {
+    if (e == cudaSuccess) return CG_OK;
+    set_error("%s failed at %s:%d: %s", what, file, line, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? CG_ENOMEM : CG_ECUDA;
+}
+
+#define CG_CUDA(call)                                                              \
+    do {                                                                           \
+        cg_status _st = ::cg::cuda_status((call), #call, __FILE__, __LINE__);      \
+        if (_st != CG_OK) return _st;                                              \
+    } while (0)
+
+#define CG_CHECK_LAUNCH(name) CG_CUDA(cudaGetLastError())
+
+#define CG_TRY(expr)                                                               \
+    do {                                                                           \
+        cg_status _st = (expr);                                                    \
+        if (_st != CG_OK) return _st;                                              \
+    } while (0)
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Grid size for a grid-stride kernel: enough blocks to fill every SM
+// `per_sm` times, never more than the work needs.
+inline unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm) {
+    uint64_t need = (n + block - 1) / block;
+    uint64_t cap = (uint64_t)sm_count() * per_sm;
+    if (need < 1) need = 1;
+    return (unsigned)(need < cap ? need : cap);
+}
+
+}  // namespace cg

@@ -1,0 +1,257 @@
+// de_kernels.cu -- distance-estimator kernels: point batches, span grids,
+// contains, loop-state dumps and the get_focii march loop.
+#include <cmath>
+
+#include "common.cuh"
+#include "de.cuh"
+#include "kernels.cuh"
+
+namespace cg {
+
+// FMA-contracted P=8 Mandelbulb (CG_NUMERICS_FAST).  Same polynomial as
+// rotate_p8 but regrouped for fused multiply-adds and approximate division
+// and square root; its loop state is not bit-identical to the reference.
+__device__ __forceinline__ float fast_sqrt(float x) {
+    return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+}
+
+__device__ __forceinline__ float mandelbulb_p8_fast(uint32_t max_iters, float bailout, float px,
+                                                    float py, float pz) {
+    float zx = px, zy = py, zz = pz, dr = 1.0f, r = 0.0f;
+    for (uint32_t i = 0; i < max_iters; ++i) {
+        const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+        r = fast_sqrt(r2);
+        if (r > bailout) break;
+        const float rr2 = r * r, rr4 = rr2 * rr2;
+        dr = fmaf(rr4 * rr2 * r * 8.0f, dr, 1.0f);
+        const float x = zx, y = zy, z = zz;
+        const float x2 = x * x, y2 = y * y, z2 = z * z;
+        const float y4 = y2 * y2;
+        const float rxy2 = x2 + y2;
+        const float rxy4 = rxy2 * rxy2;
+        // num = z8 - 28 z6 rxy2 + 70 z4 rxy4 - 28 z2 rxy6 (Horner in z2)
+        const float num = fmaf(fmaf(fmaf(z2 - 28.0f * rxy2, z2, 70.0f * rxy4), z2,
+                                    -28.0f * rxy4 * rxy2), z2, 0.0f);
+        const float a = 1.0f + __fdividef(num, rxy4 * rxy4);
+        const float X = fmaf(fmaf(fmaf(x2 - 28.0f * y2, x2, 70.0f * y4), x2, -28.0f * y4 * y2),
+                             x2, -y4 * y4);
+        const float Y = fmaf(fmaf(x2 - 7.0f * y2, x2, 7.0f * y4), x2, -y4 * y2);
+        const float Z = fmaf(z2 - 6.0f * rxy2, z2, rxy4);
+        zx = fmaf(a, X, px);
+        zy = fmaf(8.0f * a * x * y, Y, py);
+        zz = fmaf(8.0f * z * fast_sqrt(rxy2) * (z2 - rxy2), Z, pz);
+    }
+    return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
+}
+
+// Kernel modes.
+enum Mode { MODE_P8 = 0, MODE_INT = 1, MODE_POLAR = 2, MODE_SPHERE = 3, MODE_P8_FAST = 4 };
+
+template <int M>
+__device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
+    if (M == MODE_P8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_POLAR) return polar_de(s, x, y, z);
+    if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
+    return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
+}
+
+template <int M>
+__global__ void __launch_bounds__(256) k_de_points(ShapeDev s, const float* __restrict__ pts,
+                                                   uint64_t n, float* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+        out[i] = eval<M>(s, x, y, z);
+    }
+}
+
+// Corner (x, y, z) of a span grid: p = start + across * (v / res)
+// (src/mesh/buffer.rs:79-80).  v / res is exact for a power-of-two res, so it
+// is formed as v * inv_res.
+__device__ __forceinline__ void grid_point(const GridDev& g, uint32_t i, float& px, float& py,
+                                           float& pz) {
+    const uint32_t z = i % g.n;
+    const uint32_t xy = i / g.n;
+    const uint32_t y = xy % g.n;
+    const uint32_t x = xy / g.n;
+    px = __fadd_rn(g.start[0], __fmul_rn(g.across[0], __fmul_rn((float)x, g.inv_res)));
+    py = __fadd_rn(g.start[1], __fmul_rn(g.across[1], __fmul_rn((float)y, g.inv_res)));
+    pz = __fadd_rn(g.start[2], __fmul_rn(g.across[2], __fmul_rn((float)z, g.inv_res)));
+}
+
+template <int M>
+__global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* __restrict__ out) {
+    const uint32_t total = g.n * g.n * g.n;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        float x, y, z;
+        grid_point(g, i, x, y, z);
+        out[i] = eval<M>(s, x, y, z);
+    }
+}
+
+__global__ void k_state(ShapeDev s, const float* __restrict__ pts, uint64_t n,
+                        float4* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        MbState st;
+        if (s.power == 8)
+            mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, pts[3 * i], pts[3 * i + 1],
+                                       pts[3 * i + 2], &st);
+        else
+            mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, pts[3 * i],
+                                        pts[3 * i + 1], pts[3 * i + 2], &st);
+        out[i] = make_float4(st.r, st.dr, __uint_as_float(st.steps), __uint_as_float(st.escaped));
+    }
+}
+
+// Shape::contains (src/shape/mod.rs:78-80); Sphere overrides it with
+// |c - p|^2 <= r^2 (src/shape/sphere.rs:24-26).
+__global__ void k_contains(ShapeDev s, const float* __restrict__ pts, uint64_t n,
+                           uint8_t* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+        bool in;
+        if (s.kind == CG_SHAPE_SPHERE) {
+            const float dx = __fsub_rn(s.center[0], x), dy = __fsub_rn(s.center[1], y),
+                        dz = __fsub_rn(s.center[2], z);
+            const float m2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                       __fmul_rn(dz, dz));
+            in = m2 <= __fmul_rn(s.radius, s.radius);
+        } else {
+            in = shape_de(s, x, y, z) < 0.0f;
+        }
+        out[i] = in ? 1 : 0;
+    }
+}
+
+// March loop of ShapeMesh::get_focii (src/mesh/mod.rs:229-241).
+__global__ void k_march(ShapeDev s, const float* __restrict__ org, const float* __restrict__ dir,
+                        uint64_t n, uint32_t max_steps, float eps, float* __restrict__ hits,
+                        uint8_t* __restrict__ hit) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float px = org[3 * i], py = org[3 * i + 1], pz = org[3 * i + 2];
+        const float dx = dir[3 * i], dy = dir[3 * i + 1], dz = dir[3 * i + 2];
+        uint8_t h = 0;
+        for (uint32_t k = 0; k < max_steps; ++k) {
+            const float d = shape_de(s, px, py, pz);
+            px = __fadd_rn(px, __fmul_rn(dx, d));
+            py = __fadd_rn(py, __fmul_rn(dy, d));
+            pz = __fadd_rn(pz, __fmul_rn(dz, d));
+            if (d < eps) {
+                h = 1;
+                break;
+            }
+        }
+        hits[3 * i] = px;
+        hits[3 * i + 1] = py;
+        hits[3 * i + 2] = pz;
+        hit[i] = h;
+    }
+}
+
+// Rotate steps and escapes over a span grid (same loop as k_de_grid).
+template <bool P8>
+__global__ void __launch_bounds__(256) k_grid_work(ShapeDev s, GridDev g,
+                                                   unsigned long long* __restrict__ acc) {
+    const uint32_t total = g.n * g.n * g.n;
+    unsigned long long steps = 0, esc = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += gridDim.x * blockDim.x) {
+        float x, y, z;
+        grid_point(g, i, x, y, z);
+        MbState st;
+        mandelbulb_de<Exact, P8>(s.power, s.max_iters, s.bailout, x, y, z, &st);
+        steps += st.steps;
+        esc += st.escaped;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        steps += __shfl_down_sync(0xFFFFFFFFu, steps, o);
+        esc += __shfl_down_sync(0xFFFFFFFFu, esc, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], steps);
+        atomicAdd(&acc[1], esc);
+    }
+}
+
+cg_status launch_grid_work(const ShapeDev& s, const GridDev& g, unsigned long long* acc,
+                           cudaStream_t st) {
+    const uint64_t total = (uint64_t)g.n * g.n * g.n;
+    const unsigned B = 256, G = grid_for(total, B, 16);
+    if (s.power == 8)
+        k_grid_work<true><<<G, B, 0, st>>>(s, g, acc);
+    else
+        k_grid_work<false><<<G, B, 0, st>>>(s, g, acc);
+    CG_CHECK_LAUNCH("k_grid_work");
+    return CG_OK;
+}
+
+static int mode_of(const ShapeDev& s, uint32_t numerics) {
+    if (s.kind == CG_SHAPE_SPHERE) return MODE_SPHERE;
+    if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return MODE_POLAR;
+    if (s.power == 8) return numerics == CG_NUMERICS_FAST ? MODE_P8_FAST : MODE_P8;
+    return MODE_INT;
+}
+
+cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
+                           uint32_t numerics, cudaStream_t st) {
+    if (n == 0) return CG_OK;
+    const unsigned B = 256, G = grid_for(n, B, 16);
+    switch (mode_of(s, numerics)) {
+    case MODE_P8: k_de_points<MODE_P8><<<G, B, 0, st>>>(s, pts, n, out); break;
+    case MODE_INT: k_de_points<MODE_INT><<<G, B, 0, st>>>(s, pts, n, out); break;
+    case MODE_POLAR: k_de_points<MODE_POLAR><<<G, B, 0, st>>>(s, pts, n, out); break;
+    case MODE_SPHERE: k_de_points<MODE_SPHERE><<<G, B, 0, st>>>(s, pts, n, out); break;
+    default: k_de_points<MODE_P8_FAST><<<G, B, 0, st>>>(s, pts, n, out); break;
+    }
+    CG_CHECK_LAUNCH("k_de_points");
+    return CG_OK;
+}
+
+cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
+                         cudaStream_t st) {
+    const uint64_t total = (uint64_t)g.n * g.n * g.n;
+    const unsigned B = 256, G = grid_for(total, B, 16);
+    switch (mode_of(s, numerics)) {
+    case MODE_P8: k_de_grid<MODE_P8><<<G, B, 0, st>>>(s, g, out); break;
+    case MODE_INT: k_de_grid<MODE_INT><<<G, B, 0, st>>>(s, g, out); break;
+    case MODE_POLAR: k_de_grid<MODE_POLAR><<<G, B, 0, st>>>(s, g, out); break;
+    case MODE_SPHERE: k_de_grid<MODE_SPHERE><<<G, B, 0, st>>>(s, g, out); break;
+    default: k_de_grid<MODE_P8_FAST><<<G, B, 0, st>>>(s, g, out); break;
+    }
+    CG_CHECK_LAUNCH("k_de_grid");
+    return CG_OK;
+}
+
+cg_status launch_state(const ShapeDev& s, const float* pts, uint64_t n, float* out,
+                       cudaStream_t st) {
+    if (n == 0) return CG_OK;
+    const unsigned B = 256, G = grid_for(n, B, 16);
+    k_state<<<G, B, 0, st>>>(s, pts, n, reinterpret_cast<float4*>(out));
+    CG_CHECK_LAUNCH("k_state");
+    return CG_OK;
+}
+
+cg_status launch_contains(const ShapeDev& s, const float* pts, uint64_t n, uint8_t* out,
+                          cudaStream_t st) {
+    if (n == 0) return CG_OK;
+    const unsigned B = 256, G = grid_for(n, B, 16);
+    k_contains<<<G, B, 0, st>>>(s, pts, n, out);
+    CG_CHECK_LAUNCH("k_contains");
+    return CG_OK;
+}
+
+cg_status launch_march(const ShapeDev& s, const float* org, const float* dir, uint64_t n,
+                       uint32_t max_steps, float eps, float* hits, uint8_t* hit, cudaStream_t st) {
+    if (n == 0) return CG_OK;
+    const unsigned B = 128, G = grid_for(n, B, 16);
+    k_march<<<G, B, 0, st>>>(s, org, dir, n, max_steps, eps, hits, hit);
+    CG_CHECK_LAUNCH("k_march");
+    return CG_OK;
+}
+
+}  // namespace cg

@@ -1,0 +1,91 @@
+// kernels.cuh -- declarations shared between the kernel translation units
+// and the C ABI implementation.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cantucci_gpu.h"
+#include "de.cuh"
+
+namespace cg {
+
+// A span grid after the one-cell widening of src/mesh/buffer.rs:64-67.
+struct GridDev {
+    float start[3];   // widened span start
+    float across[3];  // widened span end - start
+    float inv_res;    // 1 / res (exact: res is a power of two)
+    uint32_t n;       // res + 1 corners per axis
+};
+
+// Host-side span set-up, in the reference's f32 operation order.
+struct SpanSetup {
+    float start[3], end[3];  // widened span
+    float across[3];         // end - start (buffer.rs:77)
+    float step[3];           // (end - start) / res (buffer.rs:101)
+    float delta[3];          // 0.7 * (end - start) / res (buffer.rs:257)
+};
+SpanSetup setup_span(const cg_span& span, uint32_t res);
+GridDev make_grid(const SpanSetup& su, uint32_t res);
+
+cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
+                           uint32_t numerics, cudaStream_t st);
+cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
+                         cudaStream_t st);
+cg_status launch_grid_work(const ShapeDev& s, const GridDev& g, unsigned long long* acc,
+                           cudaStream_t st);
+cg_status launch_state(const ShapeDev& s, const float* pts, uint64_t n, float* out,
+                       cudaStream_t st);
+cg_status launch_contains(const ShapeDev& s, const float* pts, uint64_t n, uint8_t* out,
+                          cudaStream_t st);
+cg_status launch_march(const ShapeDev& s, const float* org, const float* dir, uint64_t n,
+                       uint32_t max_steps, float eps, float* hits, uint8_t* hit, cudaStream_t st);
+
+// Counters the mesher kernels write on the device.
+struct MeshCounters {
+    uint32_t vertices;  // surface cells
+    uint32_t quads;     // faces
+    uint32_t status;    // bit 0: a lerp factor left [0,1]
+    uint32_t pad;
+};
+enum : uint32_t { MESH_LERP_FAIL = 1u };
+
+// Device workspace of one span mesh (sizes from mesh_workspace_layout).
+struct MeshWork {
+    float* dists;        // (res+1)^3 corner distances
+    uint32_t* sgn;       // sign words: (res+1)^2 rows x W words
+    uint32_t* cellbits;  // surface-cell words: res^2 rows x Wc words
+    uint32_t* wordoff;   // vertices before each cell word, within its row
+    uint32_t* rowcnt;    // vertices per cell row
+    uint32_t* rowoff;    // exclusive scan of rowcnt
+    uint32_t* quadcnt;   // quads per corner row
+    uint32_t* quadoff;   // exclusive scan of quadcnt
+    uint32_t* cellidx;   // cell index of each vertex (capacity res^3)
+    uint32_t* scratch;   // scan block sums
+    MeshCounters* counters;
+};
+
+struct MeshDims {
+    uint32_t res, n, W, Wc;
+};
+MeshDims mesh_dims(uint32_t res);
+// Byte size of a workspace for `res`; fills `w` with offsets from `base`.
+size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
+
+// Steps 2 and 3 of naive_surface_nets on a filled `dists` grid.  Output
+// arrays are written only up to their capacity; counts land in w.counters.
+cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                                 const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                                 uint32_t* idx, uint64_t icap, cudaStream_t st,
+                                 cudaEvent_t ev_after_vertices);
+
+// Cell -> vertex id table of the last mesh (0xFFFFFFFF off the surface).
+cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* points,
+                              cudaStream_t st);
+
+// Exclusive scan of n uint32 (n <= 16M); the total goes to *total.
+cg_status launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
+                                uint32_t* total, cudaStream_t st);
+size_t scan_scratch_words(uint32_t n);
+
+}  // namespace cg

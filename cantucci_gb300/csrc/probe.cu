@@ -1,0 +1,60 @@
+// probe.cu -- FP32 pipe peak of the current GPU, measured: the roofline
+// denominator for the distance-estimator kernels (which run on the FP32 and
+// SFU pipes, not on tensor cores).
+//
+// Every thread runs 8 independent FFMA chains, 8 warps per scheduler, one
+// full wave of CTAs per SM; the result is 2 flops per FFMA over the kernel's
+// CUDA-event time.
+#include "common.cuh"
+
+namespace cg {
+
+__global__ void __launch_bounds__(256) k_ffma_peak(float* out, uint32_t iters, float a, float b) {
+    float r0 = threadIdx.x * 1e-7f, r1 = r0 + 1e-7f, r2 = r0 + 2e-7f, r3 = r0 + 3e-7f;
+    float r4 = r0 + 4e-7f, r5 = r0 + 5e-7f, r6 = r0 + 6e-7f, r7 = r0 + 7e-7f;
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            r0 = fmaf(r0, a, b); r1 = fmaf(r1, a, b); r2 = fmaf(r2, a, b); r3 = fmaf(r3, a, b);
+            r4 = fmaf(r4, a, b); r5 = fmaf(r5, a, b); r6 = fmaf(r6, a, b); r7 = fmaf(r7, a, b);
+        }
+    }
+    const float s = ((r0 + r1) + (r2 + r3)) + ((r4 + r5) + (r6 + r7));
+    if (s == 12345.678f) out[blockIdx.x] = s;  // keeps the chains alive
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, double* flops_per_s) {
+    if (!flops_per_s || iters == 0) {
+        set_error("bad arguments");
+        return CG_EINVAL;
+    }
+    float* out = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    const unsigned blocks = (unsigned)sm_count() * 8, threads = 256;
+    cg_status st = CG_OK;
+    do {
+        if ((st = cuda_status(cudaMalloc(&out, blocks * sizeof(float)), "cudaMalloc", __FILE__,
+                              __LINE__)) != CG_OK)
+            break;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        k_ffma_peak<<<blocks, threads>>>(out, iters / 8 + 1, 0.999999f, 1e-7f);  // warm-up
+        cudaEventRecord(e0);
+        k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(e1);
+        if ((st = cuda_status(cudaEventSynchronize(e1), "k_ffma_peak", __FILE__, __LINE__)) != CG_OK)
+            break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double fmas = (double)blocks * threads * iters * 16.0 * 8.0;
+        *flops_per_s = 2.0 * fmas / (ms * 1e-3);
+    } while (0);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (out) cudaFree(out);
+    return st;
+}

@@ -1,0 +1,130 @@
+// scan.cu -- device-wide exclusive prefix sum of uint32 counts, used to turn
+// per-row surface-cell and quad counts into vertex and index offsets in the
+// reference's cube() order (src/util/iter.rs:31-51).
+//
+// Three launches: per-tile sums, one-CTA scan of the tile sums, per-tile scan
+// plus offset.  Tiles are 4096 counts (1024 threads x 4), so one top-level
+// CTA covers 4096 tiles = 16M counts, enough for res^2 rows at res <= 1024.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cg {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Exclusive scan of one value per thread across the CTA; returns the CTA total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums,
+                                                         uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        uint32_t w = lane < nw ? warp_sums[lane] : 0;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= o) wi += t;
+        }
+        if (lane < nw) warp_sums[lane] = wi - w;  // exclusive warp offsets
+        if (lane == nw - 1) warp_sums[32] = wi;   // CTA total
+    }
+    __syncthreads();
+    const uint32_t res = warp_sums[warp] + inc - v;
+    total = warp_sums[32];
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in,
+                                                              uint32_t n,
+                                                              uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t ws[33];
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+        if (base + k < n) s += in[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, ws, total);
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// One CTA: exclusive scan of the tile sums in place, total to *total.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t* __restrict__ tile_sums,
+                                                           uint32_t ntiles,
+                                                           uint32_t* __restrict__ total) {
+    __shared__ uint32_t ws[33];
+    const uint32_t base = threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = (base + k < ntiles) ? tile_sums[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t off = block_exclusive_scan(s, ws, tot);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < ntiles) tile_sums[base + k] = off;
+        off += v[k];
+    }
+    if (threadIdx.x == 0) *total = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __restrict__ in,
+                                                            uint32_t n,
+                                                            const uint32_t* __restrict__ tile_off,
+                                                            uint32_t* __restrict__ out) {
+    __shared__ uint32_t ws[33];
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t off = block_exclusive_scan(s, ws, tot) + tile_off[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < n) out[base + k] = off;
+        off += v[k];
+    }
+}
+
+size_t scan_scratch_words(uint32_t n) {
+    return (n + SCAN_TILE - 1) / SCAN_TILE + 1;
+}
+
+cg_status launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
+                                uint32_t* total, cudaStream_t st) {
+    const uint32_t ntiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (ntiles > SCAN_TILE) {
+        set_error("exclusive scan of %u counts exceeds the %u-count limit", n,
+                  SCAN_TILE * SCAN_TILE);
+        return CG_EINVAL;
+    }
+    if (n == 0) {
+        CG_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t), st));
+        return CG_OK;
+    }
+    k_scan_reduce<<<ntiles, SCAN_THREADS, 0, st>>>(in, n, scratch);
+    CG_CHECK_LAUNCH("k_scan_reduce");
+    k_scan_top<<<1, SCAN_THREADS, 0, st>>>(scratch, ntiles, total);
+    CG_CHECK_LAUNCH("k_scan_top");
+    k_scan_down<<<ntiles, SCAN_THREADS, 0, st>>>(in, n, scratch, out);
+    CG_CHECK_LAUNCH("k_scan_down");
+    return CG_OK;
+}
+
+}  // namespace cg

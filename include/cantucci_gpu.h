@@ -1,0 +1,197 @@
+/*
+ * cantucci_gpu.h -- C ABI of the GB300 (sm_103a) Mandelbulb distance
+ * estimator, span mesher and sphere tracer.
+ *
+ * Every function is `extern "C"`, takes plain pointers and sizes, and returns
+ * a cg_status.  Pointers documented as "device" are CUDA device pointers on
+ * the current device; `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Reference citations are file:line in
+ * LukasKalbertodt/cantucci; each entry point names the Rust interface it
+ * replaces.  Where the reference panics (assert!, lerp factor outside [0,1])
+ * these functions return an error status instead.
+ *
+ * Thread safety: the stateless entry points (cg_min_distance_from,
+ * cg_contains, cg_de_span_grid, cg_march, ...) may be called from any number
+ * of host threads.  A cg_mesher serialises its own calls with an internal
+ * mutex; give each worker thread its own mesher for concurrency (the
+ * reference runs generate_for_box from a thread pool, src/mesh/mod.rs:141).
+ */
+#ifndef CANTUCCI_GPU_H
+#define CANTUCCI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CG_ABI_VERSION 1
+
+typedef enum cg_status {
+    CG_OK = 0,
+    CG_EINVAL = 1,     /* invalid argument (the reference asserts and panics) */
+    CG_ECAPACITY = 2,  /* an output buffer is too small; required counts are reported */
+    CG_ELERP = 3,      /* a lerp factor left [0,1] (src/math.rs:19 panics there) */
+    CG_ECUDA = 4,      /* a CUDA call failed; see cg_last_error() */
+    CG_ENOMEM = 5,     /* device allocation failed */
+    CG_ETIMEOUT = 6,   /* a device-side wait hit its iteration limit */
+    CG_ENODEV = 7      /* no CUDA device */
+} cg_status;
+
+/* Shape kinds. */
+enum {
+    CG_SHAPE_MANDELBULB = 0,       /* Mandelbulb<const P: u8> (src/shape/mandelbulb.rs:13-91) */
+    CG_SHAPE_SPHERE = 1,           /* Sphere (src/shape/sphere.rs:5-52) */
+    CG_SHAPE_MANDELBULB_POLAR = 2  /* real-power polar form (src/shape/mandelbulb.frag:1-39) + rotation */
+};
+
+/* Numerics of the distance estimator. */
+enum {
+    CG_NUMERICS_EXACT = 0,  /* IEEE f32, reference operation order: bit-identical loop state */
+    CG_NUMERICS_FAST = 1    /* FMA-contracted, approximate div/sqrt; not bit-faithful */
+};
+
+/* Normals of the mesher. */
+enum {
+    CG_NORMALS_FD = 0,      /* six central differences, as buffer.rs:256-266 */
+    CG_NORMALS_ADJOINT = 1  /* analytic dDE/dp from the adjoint kernel (new) */
+};
+
+/* A shape; 48 bytes.  `power`/`max_iters`/`bailout` are Mandelbulb's fields
+ * (src/shape/mandelbulb.rs:13-16; the reference's u64 max_iters fits u32 here). */
+typedef struct cg_shape {
+    int32_t kind;
+    int32_t power;       /* integer power P, 1..255 (Mandelbulb<const P: u8>) */
+    float power_f;       /* real power of the polar form */
+    uint32_t max_iters;  /* >= 1 (mandelbulb.rs:20) */
+    float bailout;
+    float rot[3];        /* Euler angles (a,b,c), R = Rz(c) Ry(b) Rx(a), DE(p) = DE0(R^T p) */
+    float center[3];     /* Sphere centre */
+    float radius;        /* Sphere radius */
+} cg_shape;
+
+/* octree::Span = Range<Point3<f32>> (src/octree/mod.rs:13). */
+typedef struct cg_span {
+    float start[3];
+    float end[3];
+} cg_span;
+
+/* mesh::Vertex, #[repr(C)], 28 bytes (src/mesh/mod.rs:255-261). */
+typedef struct cg_vertex {
+    float position[3];
+    float normal[3];
+    float distance_from_surface;
+} cg_vertex;
+
+/* mesh::buffer::Timings (src/mesh/buffer.rs:398-405): stage times in ms. */
+typedef struct cg_timings {
+    float first_ms;   /* step 1: distances at every corner */
+    float second_ms;  /* step 2: surface cells, vertices, normals */
+    float third_ms;   /* step 3: quad indices */
+    uint32_t vertices;
+    uint32_t faces;
+} cg_timings;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* CG_ABI_VERSION of the loaded library. */
+int cg_abi_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* cg_last_error(void);
+/* sizeof(cg_shape), sizeof(cg_vertex): layout check for foreign callers. */
+uint32_t cg_sizeof_shape(void);
+uint32_t cg_sizeof_vertex(void);
+
+/* ---- distance estimator ----------------------------------------------- */
+
+/* Shape::batch_min_distance_from (src/shape/mod.rs:89; per point
+ * Mandelbulb::min_distance_from, src/shape/mandelbulb.rs:59-79).
+ * points: device, n x 3 floats (Point3<f32> layout); out: device, n floats. */
+cg_status cg_min_distance_from(const cg_shape* shape, const float* points, uint64_t n,
+                               float* out, uint32_t numerics, void* stream);
+
+/* Shape::contains (src/shape/mod.rs:78-80; Sphere override
+ * src/shape/sphere.rs:24-26).  out: device, n bytes of 0/1. */
+cg_status cg_contains(const cg_shape* shape, const float* points, uint64_t n, uint8_t* out,
+                      void* stream);
+
+/* Step 1 of naive_surface_nets (src/mesh/buffer.rs:63-83): the span is
+ * widened by one cell per side and the DE is evaluated at all (res+1)^3
+ * corners.  dists: device, (res+1)^3 floats, x-major, z fastest
+ * (GridTable layout, src/util/grid.rs:45-48). */
+cg_status cg_de_span_grid(const cg_shape* shape, const cg_span* span, uint32_t resolution,
+                          float* dists, uint32_t numerics, void* stream);
+
+/* Mandelbulb loop state at exit, for bit-level parity tests: stale r, dr,
+ * rotate steps (uint32 stored as float bits) and escape flag per point.
+ * state: device, n x 4 floats. */
+cg_status cg_mandelbulb_state(const cg_shape* shape, const float* points, uint64_t n,
+                              float* state, void* stream);
+
+/* ---- span mesher -------------------------------------------------------- */
+
+typedef struct cg_mesher cg_mesher;
+
+/* A mesher owns a stream, events and a grow-only device workspace. */
+cg_status cg_mesher_create(int device, cg_mesher** out);
+void cg_mesher_destroy(cg_mesher* mesher);
+/* Select the normals (CG_NORMALS_FD default). */
+cg_status cg_mesher_set_normals(cg_mesher* mesher, uint32_t normals);
+
+/* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.
+ * Writes min(count, cap) items; if a count exceeds its capacity the call
+ * returns CG_ECAPACITY with *n_vertices / *n_indices set to the required
+ * counts.  timings may be NULL. */
+cg_status cg_generate_for_box(cg_mesher* mesher, const cg_span* span, const cg_shape* shape,
+                              uint32_t resolution, cg_vertex* vertices, uint64_t vertex_cap,
+                              uint32_t* indices, uint64_t index_cap, uint64_t* n_vertices,
+                              uint64_t* n_indices, cg_timings* timings);
+
+/* Same, with DEVICE output buffers; the mesh stays on the GPU (replaces the
+ * host round trip before MeshView::new, src/mesh/view.rs:23-41). */
+cg_status cg_generate_for_box_device(cg_mesher* mesher, const cg_span* span,
+                                     const cg_shape* shape, uint32_t resolution,
+                                     cg_vertex* vertices, uint64_t vertex_cap, uint32_t* indices,
+                                     uint64_t index_cap, uint64_t* n_vertices,
+                                     uint64_t* n_indices, cg_timings* timings);
+
+/* Device pointer of the last mesh's corner distances (GridTable `dists` of
+ * buffer.rs:78, (res+1)^3 floats), valid until the mesher's next call. */
+cg_status cg_mesher_dists(cg_mesher* mesher, const float** dists, uint32_t* resolution);
+
+/* Expands the last mesh's cell -> vertex-id table (GridTable `points` of
+ * buffer.rs:113: 0xFFFFFFFF off the surface) into `points`, a DEVICE buffer
+ * of res^3 uint32, on the mesher's stream (synchronised before return). */
+cg_status cg_mesher_points(cg_mesher* mesher, uint32_t* points);
+
+/* ---- sphere tracing ----------------------------------------------------- */
+
+/* March loop of ShapeMesh::get_focii (src/mesh/mod.rs:229-241): for each ray
+ * pos += dir * DE(pos) up to max_steps times, hit when DE < epsilon.
+ * origins, dirs, hits: device n x 3 floats; hit: device n bytes. */
+cg_status cg_march(const cg_shape* shape, const float* origins, const float* dirs, uint64_t n,
+                   uint32_t max_steps, float epsilon, float* hits, uint8_t* hit,
+                   void* stream);
+
+/* ---- measurement -------------------------------------------------------- */
+
+/* The cudaStream_t (as void*) the mesher launches on, so a caller can time
+ * its calls with CUDA events on that stream. */
+cg_status cg_mesher_stream(cg_mesher* mesher, void** stream);
+
+/* Work actually done by step 1 on a span grid (the same loop as
+ * cg_de_span_grid): total rotate steps and escapes over the (res+1)^3
+ * corners of an integer-power Mandelbulb.  Synchronous. */
+cg_status cg_span_grid_work(const cg_shape* shape, const cg_span* span, uint32_t resolution,
+                            uint64_t* steps, uint64_t* escapes);
+
+/* FP32 pipe peak of the current device in flop/s (2 per FFMA), measured with
+ * a dependent-chain FFMA kernel of `iters` x 128 FFMA per thread.  No
+ * reference counterpart: the denominator of the estimator's roofline. */
+cg_status cg_fp32_peak_probe(uint32_t iters, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,176 @@
+"""GPU span mesher (MeshBuffer::generate_for_box) against goldens and oracle.
+
+Bar: the cell -> vertex-id table and the triangle index list are bit-exact
+(P=8 and Sphere); vertex positions/normals/distances, which depend on the
+final ln of the corner distances, are compared with the tolerances stated;
+the Sphere mesh (no libm at all) is bit-exact everywhere.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from cantucci_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def sha(a) -> bytes:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest()
+
+
+def as7(v):
+    return np.ascontiguousarray(v).view(np.float32).reshape(-1, 7)
+
+
+def angle_deg(a, b):
+    a = a / np.linalg.norm(a, axis=1, keepdims=True)
+    b = b / np.linalg.norm(b, axis=1, keepdims=True)
+    return np.degrees(np.arccos(np.clip(np.sum(a * b, axis=1), -1, 1)))
+
+
+@pytest.fixture(scope="module")
+def mesher(cg):
+    m = cg.Mesher(0)
+    yield m
+    m.close()
+
+
+def test_c1_topology_matches_golden(cg, golden, mesher):
+    s = cg.Mandelbulb.classic(15, 2.5)
+    buf, t = cg.MeshBuffer.generate_for_box(cg.Span(*W.SPAN_C1), s, 64, mesher=mesher)
+    assert [len(buf.vertices), len(buf.indices)] == golden["c1_counts"].tolist()
+    assert (t.vertices, t.faces * 6) == tuple(golden["c1_counts"].tolist())
+    assert sha(buf.indices) == golden["c1_indices_sha"].tobytes()
+    pts = mesher.last_points().cpu().numpy().astype(np.uint32)
+    assert sha(pts) == golden["c1_points_sha"].tobytes()
+    assert np.array_equal(buf.indices[:6000], golden["c1_index_head"])
+    v = as7(buf.vertices)[::37]
+    g = golden["c1_vertex_sample"]
+    np.testing.assert_allclose(v[:, :3], g[:, :3], rtol=0, atol=1e-6)
+    assert angle_deg(v[:, 3:6], g[:, 3:6]).max() < 0.01
+    np.testing.assert_allclose(v[:, 6], g[:, 6], rtol=1e-4, atol=1e-7)
+
+
+def test_c1_vertices_vs_oracle(cg, orc, mesher):
+    s = cg.Mandelbulb.classic(15, 2.5)
+    buf, _ = cg.MeshBuffer.generate_for_box(cg.Span(*W.SPAN_C1), s, 64, mesher=mesher)
+    ref = orc.generate_for_box(orc.mandelbulb(8, 15, 2.5), np.array(W.SPAN_C1).ravel(), 64)
+    assert np.array_equal(buf.indices, ref["indices"])
+    a, b = as7(buf.vertices), as7(ref["vertices"])
+    exact = np.all(a.view(np.uint32) == b.view(np.uint32), axis=1)
+    assert exact.mean() >= 0.9  # every vertex whose corner logf rounds like glibc's
+    np.testing.assert_allclose(a[:, :3], b[:, :3], rtol=0, atol=1e-6)
+    assert angle_deg(a[:, 3:6], b[:, 3:6]).max() < 0.01
+
+
+@pytest.mark.parametrize("n", range(6))
+def test_small_spans_match_golden(cg, golden, mesher, n):
+    P, it, rr = golden["small%d_meta" % n].tolist()
+    sp = golden["small%d_span" % n]
+    buf, _ = cg.MeshBuffer.generate_for_box(cg.Span(sp[:3], sp[3:]), cg.Mandelbulb(P, it, 2.5), rr,
+                                            mesher=mesher)
+    pts = mesher.last_points().cpu().numpy().astype(np.uint32)
+    d = mesher.last_dists().cpu().numpy()
+    gd = golden["small%d_dists" % n]
+    if P == 8:
+        assert np.array_equal(pts, golden["small%d_points" % n])
+        assert np.array_equal(buf.indices, golden["small%d_indices" % n])
+    else:
+        # Trig path: a sign may flip only where the reference's own distance
+        # is tiny compared with the cell size.
+        flip = np.signbit(d) != np.signbit(gd)
+        cell = float(np.max(sp[3:] - sp[:3])) / rr
+        assert np.all(np.abs(gd[flip]) < 1e-3 * cell), np.abs(gd[flip]).max()
+        if not flip.any():
+            assert np.array_equal(buf.indices, golden["small%d_indices" % n])
+    np.testing.assert_allclose(d, gd, rtol=1e-3, atol=1e-6)
+
+
+@pytest.mark.parametrize("n", range(2))
+def test_sphere_mesh_bit_exact(cg, golden, mesher, n):
+    meta = golden["sphere%d_meta" % n]
+    sp = golden["sphere%d_span" % n]
+    buf, _ = cg.MeshBuffer.generate_for_box(cg.Span(sp[:3], sp[3:]), cg.Sphere(meta[:3], meta[3]),
+                                            int(meta[4]), mesher=mesher)
+    assert np.array_equal(as7(buf.vertices).view(np.uint32),
+                          golden["sphere%d_vertices" % n].view(np.uint32))
+    assert np.array_equal(buf.indices, golden["sphere%d_indices" % n])
+
+
+@pytest.mark.parametrize("span,res", [(((0, 0, 0), (-1, 1, 1)), 8), (((0, 0, 0), (1, 1, 1)), 6),
+                                      (((0, 0, 0), (1, 1, 1)), 0), (((0, 0, 0), (1, 1, 1)), 1),
+                                      (((0, 0, 0), (1, 1, 1)), 2048)])
+def test_invalid_arguments(cg, mesher, span, res):
+    with pytest.raises(cg.CantucciError) as e:
+        cg.MeshBuffer.generate_for_box(cg.Span(*span), cg.Mandelbulb(8, 15, 2.5), res,
+                                       mesher=mesher)
+    assert e.value.status == 1
+
+
+def test_capacity_reported(cg, mesher):
+    s = cg.Mandelbulb(8, 15, 2.5)
+    verts = np.zeros(10, cg.VERTEX_DTYPE)
+    idx = np.zeros(12, np.uint32)
+    with pytest.raises(cg.CantucciError) as e:
+        mesher.generate(cg.Span(*W.SPAN_C1), s, 16, vertices=verts, indices=idx)
+    assert e.value.status == 2
+    full, _ = cg.MeshBuffer.generate_for_box(cg.Span(*W.SPAN_C1), s, 16, mesher=mesher)
+    # what fits was written, nothing beyond
+    assert np.array_equal(idx, full.indices[:12])
+    assert np.array_equal(verts.view(np.uint8), full.vertices[:10].view(np.uint8))
+
+
+def test_device_output_matches_host(cg, mesher):
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    host, _ = cg.MeshBuffer.generate_for_box(cg.Span(*W.SPAN_C1), s, 32, mesher=mesher)
+    v = torch.empty((32 ** 3, 7), dtype=torch.float32, device="cuda")
+    i = torch.empty(18 * 32 ** 3, dtype=torch.int32, device="cuda")
+    nv, ni, _ = mesher.generate_device(cg.Span(*W.SPAN_C1), s, 32, v, i)
+    assert (nv, ni) == (len(host.vertices), len(host.indices))
+    assert np.array_equal(v[:nv].cpu().numpy().view(np.uint32), as7(host.vertices).view(np.uint32))
+    assert np.array_equal(i[:ni].cpu().numpy().view(np.uint32), host.indices)
+
+
+def test_two_meshers_in_threads(cg):
+    """The reference meshes spans from a thread pool; each worker owns a mesher."""
+    import threading
+    spans = [cg.Span(*W.SPAN_C1)] + [cg.Span(s[:3], s[3:]) for s in W.batched_spans(6, 2)[0]]
+    results = {}
+
+    def work(k):
+        m = cg.Mesher(0)
+        out = []
+        for sp in spans:
+            b, _ = cg.MeshBuffer.generate_for_box(sp, cg.Mandelbulb(8, 15, 2.5), 32, mesher=m)
+            out.append(sha(b.indices) + sha(b.vertices))
+        m.close()
+        results[k] = out
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert results[0] == results[1]
+
+
+@pytest.mark.slow
+def test_c2_full_size_vs_oracle(cg, orc, mesher):
+    """513^3 corners: cell table and index list bit-exact against the oracle."""
+    s = cg.Mandelbulb.classic(15, 2.5)
+    n = 512 ** 3
+    verts = np.empty(4_000_000, cg.VERTEX_DTYPE)
+    idx = np.empty(30_000_000, np.uint32)
+    v, i, nv, ni, tm = mesher.generate(cg.Span(*W.SPAN_C1), s, 512, vertices=verts, indices=idx)
+    gpu_points = mesher.last_points().cpu().numpy().astype(np.uint32)
+    ref = orc.generate_for_box(orc.mandelbulb(8, 15, 2.5), np.array(W.SPAN_C1).ravel(), 512,
+                               want_grids=True, vcap=4_000_000, icap=30_000_000)
+    assert ref["rc"] == 0
+    assert (nv, ni) == (ref["nv"], ref["ni"])
+    assert np.array_equal(gpu_points, ref["points"])
+    assert np.array_equal(idx[:ni], ref["indices"])
+    a, b = as7(verts[:nv]), as7(ref["vertices"])
+    np.testing.assert_allclose(a[:, :3], b[:, :3], rtol=0, atol=1e-6)
+    assert n == gpu_points.size
