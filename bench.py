@@ -185,10 +185,11 @@ def run_ours(args, rank, world, local_rank):
     vcap, icap = max(res ** 3 // 16, 4096), max(18 * res ** 3 // 16, 65536)
     verts_d = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
     idx_d = torch.empty(icap, dtype=torch.int32, device=dev)
-    nv, ni, _ = mesher.generate_device(span, shape, res, verts_d, idx_d)
+    nv, ni, _ = mesher.generate_device(span, shape, res, verts_d, idx_d, strict=False)
+    lerp_panic = mesher.last_status == _ffi.CG_ELERP
 
     def step_device():
-        return mesher.generate_device(span, shape, res, verts_d, idx_d)
+        return mesher.generate_device(span, shape, res, verts_d, idx_d, strict=False)
 
     for _ in range(args.warmup):
         step_device()
@@ -225,13 +226,13 @@ def run_ours(args, rank, world, local_rank):
     idx_h = torch.empty(icap, dtype=torch.int32, pin_memory=True)
     verts_np = verts_h.numpy().view(cg.VERTEX_DTYPE).reshape(-1)
     idx_np = idx_h.numpy().view(np.uint32)
-    mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np)
+    mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np, strict=False)
     torch.cuda.synchronize(dev)
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
     for _ in range(args.steps):
-        mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np)
+        mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np, strict=False)
     f1.record(stream)
     f1.synchronize()
     e2e_s = f0.elapsed_time(f1) * 1e-3
@@ -284,7 +285,11 @@ def run_ours(args, rank, world, local_rank):
         "stages_ms": {"first": statistics.mean(s[0] for s in stage),
                       "second": statistics.mean(s[1] for s in stage),
                       "third": statistics.mean(s[2] for s in stage)},
-        "mesh": {"vertices": nv, "indices": ni},
+        "mesh": {"vertices": nv, "indices": ni, "reference_would_panic": lerp_panic,
+                 "panic_note": "at res 512 four corners in the y=0 plane evaluate to NaN "
+                               "(x underflows, rxy8 = 0) next to outside corners, so a lerp "
+                               "factor is NaN and src/math.rs:19 asserts; the mesh is "
+                               "completed with factor 0 there, like the oracle"},
         "de_kernel_pts_per_s": n_pts / (de_ms * 1e-3),
         "roofline": roofline, "e2e": e2e, "clocks": clk,
         "gpu_launches": LAUNCHES_PER_MESH * args.steps,

@@ -250,6 +250,7 @@ class Mesher:
         check(self._lib.cg_mesher_create(device, C.byref(h)))
         self.handle = h
         self.device = device
+        self.last_status = _ffi.CG_OK
 
     def close(self):
         if self.handle:
@@ -263,8 +264,12 @@ class Mesher:
             pass
 
     def generate(self, span: Span, shape: Shape, resolution: int, vertex_cap=None,
-                 index_cap=None, vertices=None, indices=None):
-        """Mesh into host numpy arrays (pinned torch tensors also accepted)."""
+                 index_cap=None, vertices=None, indices=None, strict: bool = True):
+        """Mesh into host numpy arrays (pinned torch tensors also accepted).
+
+        With strict=False a CG_ELERP status (a lerp factor outside [0,1],
+        where the reference panics) is returned instead of raised; the mesh
+        is complete and uses factor 0 on the offending edges."""
         r3 = resolution ** 3
         if vertices is None:
             vertex_cap = r3 if vertex_cap is None else vertex_cap
@@ -279,17 +284,23 @@ class Mesher:
         st = self._lib.cg_generate_for_box(self.handle, C.byref(span.to_c()),
                                            C.byref(shape._cshape()), resolution, vptr, vcap,
                                            iptr, icap, C.byref(nv), C.byref(ni), C.byref(tm))
-        check(st)
+        if strict or st != _ffi.CG_ELERP:
+            check(st)
+        self.last_status = st
         return vertices, indices, nv.value, ni.value, tm
 
-    def generate_device(self, span: Span, shape: Shape, resolution: int, vertices, indices):
+    def generate_device(self, span: Span, shape: Shape, resolution: int, vertices, indices,
+                        strict: bool = True):
         """Mesh into CUDA tensors: vertices (cap, 7) float32, indices (cap,) int32/uint32."""
         nv, ni = C.c_uint64(), C.c_uint64()
         tm = _ffi.CgTimings()
-        check(self._lib.cg_generate_for_box_device(
+        st = self._lib.cg_generate_for_box_device(
             self.handle, C.byref(span.to_c()), C.byref(shape._cshape()), resolution,
             C.c_void_p(vertices.data_ptr()), vertices.shape[0], C.c_void_p(indices.data_ptr()),
-            indices.numel(), C.byref(nv), C.byref(ni), C.byref(tm)))
+            indices.numel(), C.byref(nv), C.byref(ni), C.byref(tm))
+        if strict or st != _ffi.CG_ELERP:
+            check(st)
+        self.last_status = st
         return nv.value, ni.value, tm
 
     def last_dists(self):
@@ -320,7 +331,7 @@ class _DeviceView:
 
     def __init__(self, ptr: int, shape, typestr: str):
         self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
-                                         "data": (ptr, True), "version": 2}
+                                         "data": (ptr, False), "version": 2}
 
 
 def _host_ptr(arr, itemsize):

@@ -123,6 +123,10 @@ def min_distance_from(shape: Shape, points, nthreads=None) -> np.ndarray:
     return out
 
 
+def contains(shape: Shape, x, y, z) -> bool:
+    return bool(lib().orc_contains(C.byref(shape), float(x), float(y), float(z)))
+
+
 def state(shape: Shape, p):
     r, dr = C.c_float(), C.c_float()
     k, e = C.c_uint32(), C.c_uint32()

@@ -38,12 +38,21 @@ def gpu_state(cg, shape, pts):
     return out.cpu().numpy()
 
 
+def same_bits(a, b):
+    """Bit equality, except that any two NaNs match (CUDA's canonical NaN and
+    x86's default NaN differ in sign and payload inside the loop state)."""
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    nan = np.isnan(a) & np.isnan(b)
+    return bool(np.all(nan | (a.view(np.uint32) == b.view(np.uint32))))
+
+
 def test_bench_points_state_bit_exact(cg, golden):
     pts = golden["points"]
     for name, (P, it, b) in P8_SHAPES.items():
         st = gpu_state(cg, cg.Mandelbulb(P, it, b), pts)
-        assert np.array_equal(st[:, 0].view(np.uint32), golden["r_" + name].view(np.uint32)), name
-        assert np.array_equal(st[:, 1].view(np.uint32), golden["dr_" + name].view(np.uint32)), name
+        assert same_bits(st[:, 0], golden["r_" + name]), name
+        assert same_bits(st[:, 1], golden["dr_" + name]), name
         assert np.array_equal(st[:, 2].view(np.uint32), golden["steps_" + name]), name
         assert np.array_equal(st[:, 3].view(np.uint32), golden["esc_" + name]), name
 
@@ -78,7 +87,7 @@ def test_random_points_state_bit_exact_vs_oracle(cg, orc):
     s = cg.Mandelbulb(8, 15, 2.5)
     st = gpu_state(cg, s, pts)
     ref = orc.batch_state(orc.mandelbulb(8, 15, 2.5), pts)
-    assert np.array_equal(st.view(np.uint32), ref.view(np.uint32))
+    assert same_bits(st, ref)
 
 
 def test_span_grid_signs_match_golden(cg, golden):
