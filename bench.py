@@ -255,13 +255,16 @@ def run_ours(args, rank, world, local_rank):
     de_ms = statistics.mean(s[0] for s in stage)
     achieved = flops / (de_ms * 1e-3) / 1e12
     peak = C.c_double()
-    _ffi.check(lib.cg_fp32_peak_probe(20000, C.byref(peak)))
+    _ffi.check(lib.cg_fp32_peak_probe(20000, 0, C.byref(peak)))
+    peak2 = C.c_double()
+    _ffi.check(lib.cg_fp32_peak_probe(20000, 1, C.byref(peak2)))
     peak_tf = peak.value / 1e12
     roofline = {
         "bound": "fp32", "kernel": "k_de_grid", "achieved": achieved, "peak": peak_tf,
         "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
         "peak_source": "measured in this run: FFMA chains, 2 flop per FFMA (FP32 pipe peak; "
                        "not in MEASURED_PEAKS.json)",
+        "peak_packed_f32x2": peak2.value / 1e12,
         "algorithmic_flops_per_launch": flops,
         "mean_steps_per_point": steps_c.value / n_pts,
         "flop_model": "76 per P=8 iteration + 6 per escape + 4 per point (add/sub/mul/div/sqrt"

@@ -69,7 +69,7 @@ SIGNATURES = [
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
     ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),
     ("cg_span_grid_work", _i32, [_shp, _spp, _u32, C.POINTER(_u64), C.POINTER(_u64)]),
-    ("cg_fp32_peak_probe", _i32, [_u32, C.POINTER(C.c_double)]),
+    ("cg_fp32_peak_probe", _i32, [_u32, _u32, C.POINTER(C.c_double)]),
 ]
 
 _lib = None

@@ -196,9 +196,11 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     mesh_workspace_layout(res, m->work, &w);
     cudaStream_t st = m->stream;
     CG_CUDA(cudaEventRecord(m->ev[0], st));
-    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st));
+    CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
+    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
-    CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2]));
+    CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
+                                  /*signs_ready=*/true));
     CG_CUDA(cudaEventRecord(m->ev[3], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));

@@ -80,14 +80,59 @@ __device__ __forceinline__ void grid_point(const GridDev& g, uint32_t i, float& 
     pz = __fadd_rn(g.start[2], __fmul_rn(g.across[2], __fmul_rn((float)z, g.inv_res)));
 }
 
+__device__ __forceinline__ float grid_coord(const GridDev& g, int k, uint32_t v) {
+    return __fadd_rn(g.start[k], __fmul_rn(g.across[k], __fmul_rn((float)v, g.inv_res)));
+}
+
+// Small grids: one corner per thread in linear (GridTable) order.  With
+// `sgn`, also sets bit z%32 of sign word (x, y, z/32) for positive corners.
 template <int M>
-__global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* __restrict__ out,
+                                                 uint32_t* __restrict__ sgn, uint32_t W) {
     const uint32_t total = g.n * g.n * g.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
         float x, y, z;
         grid_point(g, i, x, y, z);
-        out[i] = eval<M>(s, x, y, z);
+        const float d = eval<M>(s, x, y, z);
+        out[i] = d;
+        if (sgn && !(__float_as_uint(d) >> 31)) {
+            const uint32_t zi = i % g.n, row = i / g.n;
+            atomicOr(&sgn[row * W + (zi >> 5)], 1u << (zi & 31));
+        }
+    }
+}
+
+// Large grids: each warp evaluates a 2x4x4 brick of corners (x, y, z), which
+// keeps the escape counts of a warp's lanes close (89% lane efficiency on the
+// 513^3 span vs 75% for 32 corners along z).  With `sgn`, the four z-lanes of
+// each (x, y) pair OR their sign bits together and one lane sets them in the
+// sign word with atomicOr (sgn must be zeroed first).
+template <int M>
+__global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
+                                                       float* __restrict__ out,
+                                                       uint32_t* __restrict__ sgn, uint32_t W) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n = g.n;
+    const uint32_t BX = (n + 1) >> 1, BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
+    const uint32_t bricks = BX * BY * BZ;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < bricks; b += nwarps) {
+        const uint32_t bz = b % BZ, t = b / BZ, by = t % BY, bx = t / BY;
+        const uint32_t x = 2 * bx + dx, y = 4 * by + dy, z = 4 * bz + dz;
+        const bool active = x < n && y < n && z < n;
+        uint32_t bit = 0;
+        if (active) {
+            const float d = eval<M>(s, grid_coord(g, 0, x), grid_coord(g, 1, y), grid_coord(g, 2, z));
+            out[((size_t)x * n + y) * n + z] = d;
+            bit = (__float_as_uint(d) >> 31) ? 0u : (1u << (z & 31));
+        }
+        if (sgn) {
+            bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 1);
+            bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 2);
+            if (dz == 0 && bit) atomicOr(&sgn[(x * n + y) * W + (z >> 5)], bit);
+        }
     }
 }
 
@@ -212,16 +257,27 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
     return CG_OK;
 }
 
+template <int M>
+static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, uint32_t* sgn,
+                             uint32_t W, cudaStream_t st) {
+    const unsigned B = 256;
+    if (g.n >= 33) {
+        const uint64_t bricks = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2) * ((g.n + 3) >> 2);
+        k_de_grid_brick<M><<<grid_for(bricks * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+    } else {
+        const uint64_t total = (uint64_t)g.n * g.n * g.n;
+        k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+    }
+}
+
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
-                         cudaStream_t st) {
-    const uint64_t total = (uint64_t)g.n * g.n * g.n;
-    const unsigned B = 256, G = grid_for(total, B, 16);
+                         cudaStream_t st, uint32_t* sgn, uint32_t W) {
     switch (mode_of(s, numerics)) {
-    case MODE_P8: k_de_grid<MODE_P8><<<G, B, 0, st>>>(s, g, out); break;
-    case MODE_INT: k_de_grid<MODE_INT><<<G, B, 0, st>>>(s, g, out); break;
-    case MODE_POLAR: k_de_grid<MODE_POLAR><<<G, B, 0, st>>>(s, g, out); break;
-    case MODE_SPHERE: k_de_grid<MODE_SPHERE><<<G, B, 0, st>>>(s, g, out); break;
-    default: k_de_grid<MODE_P8_FAST><<<G, B, 0, st>>>(s, g, out); break;
+    case MODE_P8: launch_grid_mode<MODE_P8>(s, g, out, sgn, W, st); break;
+    case MODE_INT: launch_grid_mode<MODE_INT>(s, g, out, sgn, W, st); break;
+    case MODE_POLAR: launch_grid_mode<MODE_POLAR>(s, g, out, sgn, W, st); break;
+    case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st); break;
+    default: launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st); break;
     }
     CG_CHECK_LAUNCH("k_de_grid");
     return CG_OK;

@@ -30,8 +30,10 @@ GridDev make_grid(const SpanSetup& su, uint32_t res);
 
 cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
                            uint32_t numerics, cudaStream_t st);
+// Step 1 on a span grid.  With `sgn` (zeroed, (res+1)^2 rows x W words) the
+// kernel also packs is_sign_positive of every corner into sign words.
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
-                         cudaStream_t st);
+                         cudaStream_t st, uint32_t* sgn = nullptr, uint32_t W = 0);
 cg_status launch_grid_work(const ShapeDev& s, const GridDev& g, unsigned long long* acc,
                            cudaStream_t st);
 cg_status launch_state(const ShapeDev& s, const float* pts, uint64_t n, float* out,
@@ -72,12 +74,13 @@ MeshDims mesh_dims(uint32_t res);
 // Byte size of a workspace for `res`; fills `w` with offsets from `base`.
 size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 
-// Steps 2 and 3 of naive_surface_nets on a filled `dists` grid.  Output
-// arrays are written only up to their capacity; counts land in w.counters.
+// Steps 2 and 3 of naive_surface_nets on a filled `dists` grid (and, with
+// signs_ready, filled sign words).  Output arrays are written only up to
+// their capacity; counts land in w.counters.
 cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
-                                 cudaEvent_t ev_after_vertices);
+                                 cudaEvent_t ev_after_vertices, bool signs_ready);
 
 // Cell -> vertex id table of the last mesh (0xFFFFFFFF off the surface).
 cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* points,

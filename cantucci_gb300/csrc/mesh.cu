@@ -365,10 +365,10 @@ cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* po
 cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
-                                 cudaEvent_t ev_after_vertices) {
+                                 cudaEvent_t ev_after_vertices, bool signs_ready) {
     const uint32_t rows = d.res * d.res;
     CG_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(MeshCounters), st));
-    {
+    if (!signs_ready) {
         const uint64_t warps = (uint64_t)d.n * d.n * d.W;
         const unsigned B = 256, G = grid_for(warps * 32, B, 8);
         k_sign_words<<<G, B, 0, st>>>(w.dists, d.n, d.W, w.sgn);

@@ -23,11 +23,41 @@ __global__ void __launch_bounds__(256) k_ffma_peak(float* out, uint32_t iters, f
     if (s == 12345.678f) out[blockIdx.x] = s;  // keeps the chains alive
 }
 
+// Same work with packed two-lane instructions (fma.rn.f32x2): 4 packed chains
+// of 2 lanes = 8 scalar chains per thread.
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__global__ void __launch_bounds__(256) k_ffma2_peak(float* out, uint32_t iters, float a, float b) {
+    const float t = threadIdx.x * 1e-7f;
+    unsigned long long r0 = pack2(t, t + 1e-7f), r1 = pack2(t + 2e-7f, t + 3e-7f);
+    unsigned long long r2 = pack2(t + 4e-7f, t + 5e-7f), r3 = pack2(t + 6e-7f, t + 7e-7f);
+    const unsigned long long A = pack2(a, a), B = pack2(b, b);
+    for (uint32_t i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            r0 = fma2(r0, A, B); r1 = fma2(r1, A, B); r2 = fma2(r2, A, B); r3 = fma2(r3, A, B);
+        }
+    }
+    const unsigned long long s = r0 ^ r1 ^ r2 ^ r3;
+    if (s == 0x123456789ull) out[blockIdx.x] = 1.0f;  // keeps the chains alive
+}
+
 }  // namespace cg
 
 using namespace cg;
 
-extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, double* flops_per_s) {
+extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, uint32_t packed, double* flops_per_s) {
     if (!flops_per_s || iters == 0) {
         set_error("bad arguments");
         return CG_EINVAL;
@@ -42,9 +72,14 @@ extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, double* flops_per_s) {
             break;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        k_ffma_peak<<<blocks, threads>>>(out, iters / 8 + 1, 0.999999f, 1e-7f);  // warm-up
-        cudaEventRecord(e0);
-        k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+        for (int rep = 0; rep < 2; ++rep) {  // rep 0 warms up
+            if (rep) cudaEventRecord(e0);
+            const uint32_t it = rep ? iters : iters / 8 + 1;
+            if (packed)
+                k_ffma2_peak<<<blocks, threads>>>(out, it, 0.999999f, 1e-7f);
+            else
+                k_ffma_peak<<<blocks, threads>>>(out, it, 0.999999f, 1e-7f);
+        }
         cudaEventRecord(e1);
         if ((st = cuda_status(cudaEventSynchronize(e1), "k_ffma_peak", __FILE__, __LINE__)) != CG_OK)
             break;
