@@ -67,6 +67,7 @@ SIGNATURES = [
     ("cg_mesher_dists", _i32, [_vp, C.POINTER(_vp), C.POINTER(_u32)]),
     ("cg_mesher_points", _i32, [_vp, _vp]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
+    ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),
     ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),
     ("cg_span_grid_work", _i32, [_shp, _spp, _u32, C.POINTER(_u64), C.POINTER(_u64)]),
     ("cg_fp32_peak_probe", _i32, [_u32, _u32, C.POINTER(C.c_double)]),

@@ -189,6 +189,147 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
     return x86_nan(O::div(O::mul(0.5f, ln_r), dr));
 }
 
+// ---- two points per thread with packed IEEE instructions ----------------
+//
+// sm_100+ executes add/sub/mul.rn.f32x2 on a pair of f32 lanes in one
+// instruction; each lane is rounded exactly like the scalar .rn operation, so
+// running two points through the same source-order expression keeps both
+// bit-identical to the reference.  Division and square root stay scalar
+// (__fdiv_rn / __fsqrt_rn) per lane.
+typedef unsigned long long u64;
+
+struct X2 {
+    static __device__ __forceinline__ u64 pk(float a, float b) {
+        u64 r;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+        return r;
+    }
+    static __device__ __forceinline__ void up(u64 v, float& a, float& b) {
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+    }
+    static __device__ __forceinline__ u64 mul(u64 a, u64 b) {
+        u64 d;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+        return d;
+    }
+    static __device__ __forceinline__ u64 add(u64 a, u64 b) {
+        u64 d;
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+        return d;
+    }
+    static __device__ __forceinline__ u64 sub(u64 a, u64 b) {
+        u64 d;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+        return d;
+    }
+    static __device__ __forceinline__ u64 div(u64 a, u64 b) {
+        float a0, a1, b0, b1;
+        up(a, a0, a1);
+        up(b, b0, b1);
+        return pk(__fdiv_rn(a0, b0), __fdiv_rn(a1, b1));
+    }
+    static __device__ __forceinline__ u64 sqrt(u64 a) {
+        float a0, a1;
+        up(a, a0, a1);
+        return pk(__fsqrt_rn(a0), __fsqrt_rn(a1));
+    }
+    static __device__ __forceinline__ u64 splat(float c) { return pk(c, c); }
+};
+
+// rotate_inner_p8_scalar (mandelbulb.rs:148-200) on two points at once.
+__device__ __forceinline__ void rotate_p8_x2(u64 x, u64 y, u64 z, u64& ox, u64& oy, u64& oz) {
+    typedef X2 O;
+    const u64 c28 = O::splat(28.0f), c70 = O::splat(70.0f), c7 = O::splat(7.0f);
+    const u64 c8 = O::splat(8.0f), c6 = O::splat(6.0f), c1 = O::splat(1.0f);
+    const u64 x2 = O::mul(x, x), x4 = O::mul(x2, x2), x6 = O::mul(x4, x2), x8 = O::mul(x4, x4);
+    const u64 y2 = O::mul(y, y), y4 = O::mul(y2, y2), y6 = O::mul(y4, y2), y8 = O::mul(y4, y4);
+    const u64 z2 = O::mul(z, z), z4 = O::mul(z2, z2), z6 = O::mul(z4, z2), z8 = O::mul(z4, z4);
+    const u64 rxy2 = O::add(x2, y2);
+    const u64 rxy4 = O::mul(rxy2, rxy2);
+    const u64 rxy6 = O::mul(rxy2, rxy4);
+    const u64 rxy8 = O::mul(rxy4, rxy4);
+    const u64 num = O::sub(O::add(O::sub(z8, O::mul(O::mul(c28, z6), rxy2)),
+                                  O::mul(O::mul(c70, z4), rxy4)),
+                           O::mul(O::mul(c28, z2), rxy6));
+    const u64 a = O::add(c1, O::div(num, rxy8));
+    const u64 X = O::sub(O::sub(O::add(O::sub(x8, O::mul(O::mul(c28, x6), y2)),
+                                       O::mul(O::mul(c70, x4), y4)),
+                                O::mul(O::mul(c28, x2), y6)),
+                         y8);
+    ox = O::mul(a, X);
+    const u64 Y = O::sub(O::add(O::sub(x6, O::mul(O::mul(c7, x4), y2)), O::mul(O::mul(c7, x2), y4)),
+                         y6);
+    oy = O::mul(O::mul(O::mul(O::mul(c8, a), x), y), Y);
+    const u64 Z = O::add(O::sub(z4, O::mul(O::mul(c6, z2), rxy2)), rxy4);
+    oz = O::mul(O::mul(O::mul(O::mul(c8, z), O::sqrt(rxy2)), O::sub(z2, rxy2)), Z);
+}
+
+// Mandelbulb<8>::min_distance_from for points A and B together.  A lane
+// whose point has escaped (or is inactive) keeps iterating in lock-step with
+// garbage that is never read; its r and dr were captured when it stopped.
+__device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailout, bool liveA,
+                                                 bool liveB, float pxA, float pyA, float pzA,
+                                                 float pxB, float pyB, float pzB, float& dA,
+                                                 float& dB) {
+    typedef X2 O;
+    const u64 px = O::pk(pxA, pxB), py = O::pk(pyA, pyB), pz = O::pk(pzA, pzB);
+    const u64 c1 = O::splat(1.0f), c8 = O::splat(8.0f);
+    u64 zx = px, zy = py, zz = pz, dr = c1;
+    float rA = 0.0f, rB = 0.0f, drA = 1.0f, drB = 1.0f;
+    bool aA = liveA, aB = liveB;
+    for (uint32_t i = 0; i < max_iters; ++i) {
+        const u64 m2 = O::add(O::add(O::mul(zx, zx), O::mul(zy, zy)), O::mul(zz, zz));
+        float mA, mB, d0, d1;
+        O::up(m2, mA, mB);
+        O::up(dr, d0, d1);
+        if (aA) {
+            rA = __fsqrt_rn(mA);
+            if (rA > bailout) {
+                aA = false;
+                drA = d0;
+            }
+        }
+        if (aB) {
+            rB = __fsqrt_rn(mB);
+            if (rB > bailout) {
+                aB = false;
+                drB = d1;
+            }
+        }
+        if (!(aA || aB)) break;
+        const u64 r = O::pk(rA, rB);
+        const u64 r2 = O::mul(r, r), r4 = O::mul(r2, r2);
+        const u64 r7 = O::mul(O::mul(r, r2), r4);  // powi(r, 7): (r * r^2) * r^4
+        dr = O::add(O::mul(O::mul(r7, c8), dr), c1);
+        u64 nx, ny, nz;
+        rotate_p8_x2(zx, zy, zz, nx, ny, nz);
+        float xA, xB, yA, yB;
+        O::up(zx, xA, xB);
+        O::up(zy, yA, yB);
+        if ((aA && on_z_axis(xA, yA)) || (aB && on_z_axis(xB, yB))) {
+            float zA, zB, oxA, oxB, oyA, oyB, ozA, ozB;
+            O::up(zz, zA, zB);
+            O::up(nx, oxA, oxB);
+            O::up(ny, oyA, oyB);
+            O::up(nz, ozA, ozB);
+            if (aA && on_z_axis(xA, yA)) rotate_axis<Exact>(8, xA, yA, zA, oxA, oyA, ozA);
+            if (aB && on_z_axis(xB, yB)) rotate_axis<Exact>(8, xB, yB, zB, oxB, oyB, ozB);
+            nx = O::pk(oxA, oxB);
+            ny = O::pk(oyA, oyB);
+            nz = O::pk(ozA, ozB);
+        }
+        zx = O::add(nx, px);
+        zy = O::add(ny, py);
+        zz = O::add(nz, pz);
+    }
+    float d0, d1;
+    O::up(dr, d0, d1);
+    if (aA) drA = d0;
+    if (aB) drB = d1;
+    dA = x86_nan(__fdiv_rn(__fmul_rn(0.5f, __fmul_rn(logf(rA), rA)), drA));
+    dB = x86_nan(__fdiv_rn(__fmul_rn(0.5f, __fmul_rn(logf(rB), rB)), drB));
+}
+
 // Polar form of src/shape/mandelbulb.frag:1-39 with a real power, evaluated
 // at q = R^T p.  GLSL length() is taken as sqrt((x*x + y*y) + z*z).
 __device__ __forceinline__ float polar_de(const ShapeDev& s, float px, float py, float pz) {

@@ -257,11 +257,68 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
     return CG_OK;
 }
 
+// P=8 exact, two corners per thread with packed f32x2 instructions: each
+// warp evaluates a 4x4x4 brick, lane (dx, dy, dz) taking corners (x, y, z)
+// and (x + 2, y, z).  Sign words as in k_de_grid_brick.
+__global__ void __launch_bounds__(256) k_de_grid_p8x2(ShapeDev s, GridDev g,
+                                                      float* __restrict__ out,
+                                                      uint32_t* __restrict__ sgn, uint32_t W) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n = g.n;
+    const uint32_t B4 = (n + 3) >> 2;
+    const uint32_t bricks = B4 * B4 * B4;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < bricks; b += nwarps) {
+        const uint32_t bz = b % B4, t = b / B4, by = t % B4, bx = t / B4;
+        const uint32_t xA = 4 * bx + dx, xB = xA + 2, y = 4 * by + dy, z = 4 * bz + dz;
+        const bool inYZ = y < n && z < n;
+        const bool liveA = inYZ && xA < n, liveB = inYZ && xB < n;
+        const float py = grid_coord(g, 1, y), pz = grid_coord(g, 2, z);
+        float dA = 0.0f, dB = 0.0f;
+        if (liveA || liveB)
+            mandelbulb_p8_x2(s.max_iters, s.bailout, liveA, liveB, grid_coord(g, 0, xA), py, pz,
+                             grid_coord(g, 0, xB), py, pz, dA, dB);
+        uint32_t bitA = 0, bitB = 0;
+        if (liveA) {
+            out[((size_t)xA * n + y) * n + z] = dA;
+            bitA = (__float_as_uint(dA) >> 31) ? 0u : (1u << (z & 31));
+        }
+        if (liveB) {
+            out[((size_t)xB * n + y) * n + z] = dB;
+            bitB = (__float_as_uint(dB) >> 31) ? 0u : (1u << (z & 31));
+        }
+        if (sgn) {
+            bitA |= __shfl_xor_sync(0xFFFFFFFFu, bitA, 1);
+            bitA |= __shfl_xor_sync(0xFFFFFFFFu, bitA, 2);
+            bitB |= __shfl_xor_sync(0xFFFFFFFFu, bitB, 1);
+            bitB |= __shfl_xor_sync(0xFFFFFFFFu, bitB, 2);
+            if (dz == 0 && bitA) atomicOr(&sgn[(xA * n + y) * W + (z >> 5)], bitA);
+            if (dz == 0 && bitB) atomicOr(&sgn[(xB * n + y) * W + (z >> 5)], bitB);
+        }
+    }
+}
+
+// Kernel choice for step 1 (cg_set_option "de_grid_kernel").
+static int g_de_grid_kernel = DE_GRID_AUTO;
+
+int set_de_grid_kernel(int v) {
+    if (v < DE_GRID_AUTO || v > DE_GRID_PACKED) return 0;
+    g_de_grid_kernel = v;
+    return 1;
+}
+
 template <int M>
 static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, uint32_t* sgn,
                              uint32_t W, cudaStream_t st) {
     const unsigned B = 256;
-    if (g.n >= 33) {
+    int k = g_de_grid_kernel;
+    if (k == DE_GRID_AUTO) k = g.n >= 33 ? (M == MODE_P8 ? DE_GRID_PACKED : DE_GRID_BRICK)
+                                         : DE_GRID_LINEAR;
+    if (k == DE_GRID_PACKED && M == MODE_P8) {
+        const uint64_t b4 = (g.n + 3) >> 2;
+        k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+    } else if (k != DE_GRID_LINEAR) {
         const uint64_t bricks = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2) * ((g.n + 3) >> 2);
         k_de_grid_brick<M><<<grid_for(bricks * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
     } else {

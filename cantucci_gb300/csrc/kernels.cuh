@@ -30,6 +30,10 @@ GridDev make_grid(const SpanSetup& su, uint32_t res);
 
 cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
                            uint32_t numerics, cudaStream_t st);
+// Step-1 kernel variants (cg_set_option "de_grid_kernel").
+enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3 };
+int set_de_grid_kernel(int v);
+
 // Step 1 on a span grid.  With `sgn` (zeroed, (res+1)^2 rows x W words) the
 // kernel also packs is_sign_positive of every corner into sign words.
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,

@@ -176,6 +176,12 @@ cg_status cg_march(const cg_shape* shape, const float* origins, const float* dir
 
 /* ---- measurement -------------------------------------------------------- */
 
+/* Process-wide tuning knobs.  "de_grid_kernel": 0 auto, 1 one corner per
+ * thread in GridTable order, 2 one 2x4x4 brick per warp, 3 (P=8 only) one
+ * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic.
+ * All variants give bit-identical results. */
+cg_status cg_set_option(const char* name, int64_t value);
+
 /* The cudaStream_t (as void*) the mesher launches on, so a caller can time
  * its calls with CUDA events on that stream. */
 cg_status cg_mesher_stream(cg_mesher* mesher, void** stream);

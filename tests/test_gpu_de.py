@@ -104,6 +104,39 @@ def test_span_grid_signs_match_golden(cg, golden):
     assert ulp_diff(sample[~nan], g[~nan]).max() <= DE_ULPS
 
 
+def set_grid_kernel(v):
+    import ctypes as C
+    from cantucci_gb300 import _ffi
+    _ffi.check(_ffi.load().cg_set_option(b"de_grid_kernel", v))
+
+
+@pytest.mark.parametrize("res", [16, 64, 128])
+def test_grid_kernel_variants_bit_identical(cg, golden, res):
+    """Linear, 2x4x4-brick and packed 4x4x4-brick step-1 kernels agree bit
+    for bit, on the distances and (through the mesher) on the sign words."""
+    import torch
+    s = cg.Mandelbulb.classic(15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    outs, meshes = [], []
+    try:
+        for v in (1, 2, 3):
+            set_grid_kernel(v)
+            d = s.span_grid(span, res)
+            torch.cuda.synchronize()
+            outs.append(d.cpu().numpy().view(np.uint32))
+            buf, _ = cg.MeshBuffer.generate_for_box(span, s, res)
+            meshes.append(buf.indices)
+    finally:
+        set_grid_kernel(0)
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+    for m in meshes[1:]:
+        assert np.array_equal(m, meshes[0])
+    if res == 64:
+        assert np.array_equal(np.packbits(np.signbit(outs[0].view(np.float32)).ravel()),
+                              golden["c1_signbits"])
+
+
 def test_span_grid_vs_fp64(cg, orc):
     """Distances of the 65^3 grid against the FP64 oracle.  The GPU loop is
     bit-identical to the reference's f32 loop, so these statistics are the
