@@ -313,8 +313,7 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
                              uint32_t W, cudaStream_t st) {
     const unsigned B = 256;
     int k = g_de_grid_kernel;
-    if (k == DE_GRID_AUTO) k = g.n >= 33 ? (M == MODE_P8 ? DE_GRID_PACKED : DE_GRID_BRICK)
-                                         : DE_GRID_LINEAR;
+    if (k == DE_GRID_AUTO) k = g.n >= 33 ? DE_GRID_BRICK : DE_GRID_LINEAR;
     if (k == DE_GRID_PACKED && M == MODE_P8) {
         const uint64_t b4 = (g.n + 3) >> 2;
         k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
