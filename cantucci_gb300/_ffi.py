@@ -64,6 +64,7 @@ SIGNATURES = [
                                    C.POINTER(_u64), C.POINTER(_u64), _tmp]),
     ("cg_generate_for_box_device", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
                                           C.POINTER(_u64), C.POINTER(_u64), _tmp]),
+    ("cg_generate_for_box_noalloc", _i32, [_spp, _shp, _u32, _vp, _u64, _vp, _u64, _vp, _vp]),
     ("cg_mesher_dists", _i32, [_vp, C.POINTER(_vp), C.POINTER(_u32)]),
     ("cg_mesher_points", _i32, [_vp, _vp]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),

@@ -156,6 +156,25 @@ cg_status cg_generate_for_box_device(cg_mesher* mesher, const cg_span* span,
                                      uint64_t index_cap, uint64_t* n_vertices,
                                      uint64_t* n_indices, cg_timings* timings);
 
+/* generate_for_box for callers that must not allocate device memory: code
+ * running under CUDA-graph stream capture, engines whose allocator owns all
+ * device memory, and per-frame LOD loops that cannot take cudaMalloc's
+ * synchronisation.  No counterpart in the reference (which allocates Vecs per
+ * call).  Uses a fixed 3 MiB __device__ workspace inside the library instead
+ * of a cg_mesher, so resolution is limited to 64 (cantucci's leaf resolution,
+ * src/mesh/mod.rs:133); larger values return CG_EINVAL.  Every GPU that loads
+ * the library holds the 3 MiB until exit.  The first call on a device looks
+ * the workspace up (cudaGetSymbolAddress) and should come before any stream
+ * capture.  All calls share the workspace: calls that overlap on the GPU race,
+ * so serialise them.  Asynchronous on `stream`: vertices/indices (DEVICE, up
+ * to their capacities) and counts (DEVICE, 3 x uint32: vertices, quads,
+ * status bit 0 = a lerp factor left [0,1]) are valid once the stream reaches
+ * this point; indices hold 6 x quads entries. */
+cg_status cg_generate_for_box_noalloc(const cg_span* span, const cg_shape* shape,
+                                      uint32_t resolution, cg_vertex* vertices,
+                                      uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                                      uint32_t* counts, void* stream);
+
 /* Device pointer of the last mesh's corner distances (GridTable `dists` of
  * buffer.rs:78, (res+1)^3 floats), valid until the mesher's next call. */
 cg_status cg_mesher_dists(cg_mesher* mesher, const float** dists, uint32_t* resolution);
