@@ -42,6 +42,15 @@ class CgTimings(C.Structure):
                 ("vertices", C.c_uint32), ("faces", C.c_uint32)]
 
 
+class CgSpanJob(C.Structure):
+    _fields_ = [("span", CgSpan), ("resolution", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class CgJobMesh(C.Structure):
+    _fields_ = [("vertex_offset", C.c_uint64), ("index_offset", C.c_uint64),
+                ("vertices", C.c_uint32), ("indices", C.c_uint32)]
+
+
 VERTEX_DTYPE = np.dtype([("position", "<f4", (3,)), ("normal", "<f4", (3,)),
                          ("distance_from_surface", "<f4")])
 
@@ -67,6 +76,11 @@ SIGNATURES = [
     ("cg_generate_for_box_noalloc", _i32, [_spp, _shp, _u32, _vp, _u64, _vp, _u64, _vp, _vp]),
     ("cg_mesher_dists", _i32, [_vp, C.POINTER(_vp), C.POINTER(_u32)]),
     ("cg_mesher_points", _i32, [_vp, _vp]),
+    ("cg_batch_create", _i32, [_i32, _vp, _u32, _u64, C.POINTER(_vp)]),
+    ("cg_batch_destroy", None, [_vp]),
+    ("cg_batch_mesh", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
+    ("cg_batch_mesh_graph", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
+    ("cg_batch_dists", _i32, [_vp, _u32, C.POINTER(_vp)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
     ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),
     ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),

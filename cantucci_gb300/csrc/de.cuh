@@ -191,11 +191,17 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
 
 // ---- two points per thread with packed IEEE instructions ----------------
 //
-// sm_100+ executes add/sub/mul.rn.f32x2 on a pair of f32 lanes in one
-// instruction; each lane is rounded exactly like the scalar .rn operation, so
-// running two points through the same source-order expression keeps both
-// bit-identical to the reference.  Division and square root stay scalar
-// (__fdiv_rn / __fsqrt_rn) per lane.
+// sm_100+ executes add/sub/mul/fma.rn.f32x2 on a pair of f32 lanes in one
+// instruction, each lane rounded like the scalar .rn operation.  ptxas
+// (CUDA 13.0, sm_103a) however fuses a packed multiply whose only use is a
+// packed add or subtract into a single fused multiply-add -- one rounding
+// instead of the reference's two -- even with .rn and --fmad=false; it
+// leaves fma.rn.f32x2(q, -1, c) alone.  So every sum that has a single-use
+// product p as an operand is written as c - q with q = -p formed exactly (a
+// negated constant factor: round-to-nearest is symmetric in sign) and
+// evaluated as fma(q, -1, c), which rounds exactly like c + p.  Products
+// that feed several operations (x^2, y^2, z^2, x^6, z^4, rxy^4) keep plain
+// adds.  Division and square root stay scalar (__fdiv_rn / __fsqrt_rn).
 typedef unsigned long long u64;
 
 struct X2 {
@@ -207,6 +213,7 @@ struct X2 {
     static __device__ __forceinline__ void up(u64 v, float& a, float& b) {
         asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
     }
+    static __device__ __forceinline__ u64 splat(float c) { return pk(c, c); }
     static __device__ __forceinline__ u64 mul(u64 a, u64 b) {
         u64 d;
         asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -222,6 +229,12 @@ struct X2 {
         asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
         return d;
     }
+    // c - q, one rounding, for a q that is a single-use product.
+    static __device__ __forceinline__ u64 rsub(u64 c, u64 q) {
+        u64 d;
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(q), "l"(splat(-1.0f)), "l"(c));
+        return d;
+    }
     static __device__ __forceinline__ u64 div(u64 a, u64 b) {
         float a0, a1, b0, b1;
         up(a, a0, a1);
@@ -233,35 +246,44 @@ struct X2 {
         up(a, a0, a1);
         return pk(__fsqrt_rn(a0), __fsqrt_rn(a1));
     }
-    static __device__ __forceinline__ u64 splat(float c) { return pk(c, c); }
 };
 
-// rotate_inner_p8_scalar (mandelbulb.rs:148-200) on two points at once.
-__device__ __forceinline__ void rotate_p8_x2(u64 x, u64 y, u64 z, u64& ox, u64& oy, u64& oz) {
+// rotate_inner_p8_scalar (mandelbulb.rs:148-200) on two points at once,
+// returning the NEGATED result (-x', -y', -z') so that the caller's "+ p"
+// can be a fusion-proof subtraction.  x2 = x*x, y2 = y*y, z2 = z*z are
+// passed in (they are also the magnitude's products); rxy2 = x2 + y2.
+__device__ __forceinline__ void rotate_p8_x2_neg(u64 x, u64 y, u64 z, u64 x2, u64 y2, u64 z2,
+                                                 u64 rxy2, u64& nox, u64& noy, u64& noz) {
     typedef X2 O;
-    const u64 c28 = O::splat(28.0f), c70 = O::splat(70.0f), c7 = O::splat(7.0f);
-    const u64 c8 = O::splat(8.0f), c6 = O::splat(6.0f), c1 = O::splat(1.0f);
-    const u64 x2 = O::mul(x, x), x4 = O::mul(x2, x2), x6 = O::mul(x4, x2), x8 = O::mul(x4, x4);
-    const u64 y2 = O::mul(y, y), y4 = O::mul(y2, y2), y6 = O::mul(y4, y2), y8 = O::mul(y4, y4);
-    const u64 z2 = O::mul(z, z), z4 = O::mul(z2, z2), z6 = O::mul(z4, z2), z8 = O::mul(z4, z4);
-    const u64 rxy2 = O::add(x2, y2);
+    const u64 c28 = O::splat(28.0f), m70 = O::splat(-70.0f), c7 = O::splat(7.0f);
+    const u64 m7 = O::splat(-7.0f), m8 = O::splat(-8.0f), c6 = O::splat(6.0f);
+    const u64 x4 = O::mul(x2, x2), x6 = O::mul(x4, x2), x8 = O::mul(x4, x4);
+    const u64 y4 = O::mul(y2, y2), y6 = O::mul(y4, y2), y8 = O::mul(y4, y4);
+    const u64 z4 = O::mul(z2, z2), z6 = O::mul(z4, z2), z8 = O::mul(z4, z4);
     const u64 rxy4 = O::mul(rxy2, rxy2);
     const u64 rxy6 = O::mul(rxy2, rxy4);
     const u64 rxy8 = O::mul(rxy4, rxy4);
-    const u64 num = O::sub(O::add(O::sub(z8, O::mul(O::mul(c28, z6), rxy2)),
-                                  O::mul(O::mul(c70, z4), rxy4)),
-                           O::mul(O::mul(c28, z2), rxy6));
-    const u64 a = O::add(c1, O::div(num, rxy8));
-    const u64 X = O::sub(O::sub(O::add(O::sub(x8, O::mul(O::mul(c28, x6), y2)),
-                                       O::mul(O::mul(c70, x4), y4)),
-                                O::mul(O::mul(c28, x2), y6)),
-                         y8);
-    ox = O::mul(a, X);
-    const u64 Y = O::sub(O::add(O::sub(x6, O::mul(O::mul(c7, x4), y2)), O::mul(O::mul(c7, x2), y4)),
-                         y6);
-    oy = O::mul(O::mul(O::mul(O::mul(c8, a), x), y), Y);
-    const u64 Z = O::add(O::sub(z4, O::mul(O::mul(c6, z2), rxy2)), rxy4);
-    oz = O::mul(O::mul(O::mul(O::mul(c8, z), O::sqrt(rxy2)), O::sub(z2, rxy2)), Z);
+    // num = ((z8 - (28 z6) rxy2) + (70 z4) rxy4) - (28 z2) rxy6
+    const u64 num = O::rsub(O::rsub(O::rsub(z8, O::mul(O::mul(c28, z6), rxy2)),
+                                    O::mul(O::mul(m70, z4), rxy4)),
+                            O::mul(O::mul(c28, z2), rxy6));
+    const u64 q = O::div(num, rxy8);
+    const u64 a = O::add(O::splat(1.0f), q);    // 1 + q
+    const u64 na = O::sub(O::splat(-1.0f), q);  // -(1 + q), exactly
+    // X = (((x8 - (28 x6) y2) + (70 x4) y4) - (28 x2) y6) - y8
+    const u64 X = O::rsub(O::rsub(O::rsub(O::rsub(x8, O::mul(O::mul(c28, x6), y2)),
+                                          O::mul(O::mul(m70, x4), y4)),
+                                  O::mul(O::mul(c28, x2), y6)),
+                          y8);
+    nox = O::mul(na, X);
+    // Y = ((x6 - (7 x4) y2) + (7 x2) y4) - y6
+    const u64 Y = O::rsub(O::rsub(O::rsub(x6, O::mul(O::mul(c7, x4), y2)),
+                                  O::mul(O::mul(m7, x2), y4)),
+                          y6);
+    noy = O::mul(O::mul(O::mul(O::mul(m8, a), x), y), Y);
+    // Z = (z4 - (6 z2) rxy2) + rxy4
+    const u64 Z = O::add(O::rsub(z4, O::mul(O::mul(c6, z2), rxy2)), rxy4);
+    noz = O::mul(O::mul(O::mul(O::mul(m8, z), O::sqrt(rxy2)), O::sub(z2, rxy2)), Z);
 }
 
 // Mandelbulb<8>::min_distance_from for points A and B together.  A lane
@@ -273,12 +295,14 @@ __device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailo
                                                  float& dB) {
     typedef X2 O;
     const u64 px = O::pk(pxA, pxB), py = O::pk(pyA, pyB), pz = O::pk(pzA, pzB);
-    const u64 c1 = O::splat(1.0f), c8 = O::splat(8.0f);
+    const u64 c1 = O::splat(1.0f), m8 = O::splat(-8.0f);
     u64 zx = px, zy = py, zz = pz, dr = c1;
     float rA = 0.0f, rB = 0.0f, drA = 1.0f, drB = 1.0f;
     bool aA = liveA, aB = liveB;
     for (uint32_t i = 0; i < max_iters; ++i) {
-        const u64 m2 = O::add(O::add(O::mul(zx, zx), O::mul(zy, zy)), O::mul(zz, zz));
+        const u64 x2 = O::mul(zx, zx), y2 = O::mul(zy, zy), z2 = O::mul(zz, zz);
+        const u64 rxy2 = O::add(x2, y2);
+        const u64 m2 = O::add(rxy2, z2);  // Vec3::magnitude: (x*x + y*y) + z*z
         float mA, mB, d0, d1;
         O::up(m2, mA, mB);
         O::up(dr, d0, d1);
@@ -300,9 +324,9 @@ __device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailo
         const u64 r = O::pk(rA, rB);
         const u64 r2 = O::mul(r, r), r4 = O::mul(r2, r2);
         const u64 r7 = O::mul(O::mul(r, r2), r4);  // powi(r, 7): (r * r^2) * r^4
-        dr = O::add(O::mul(O::mul(r7, c8), dr), c1);
+        dr = O::rsub(c1, O::mul(O::mul(r7, m8), dr));  // ((r^7 * 8) * dr) + 1
         u64 nx, ny, nz;
-        rotate_p8_x2(zx, zy, zz, nx, ny, nz);
+        rotate_p8_x2_neg(zx, zy, zz, x2, y2, z2, rxy2, nx, ny, nz);
         float xA, xB, yA, yB;
         O::up(zx, xA, xB);
         O::up(zy, yA, yB);
@@ -312,15 +336,25 @@ __device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailo
             O::up(nx, oxA, oxB);
             O::up(ny, oyA, oyB);
             O::up(nz, ozA, ozB);
-            if (aA && on_z_axis(xA, yA)) rotate_axis<Exact>(8, xA, yA, zA, oxA, oyA, ozA);
-            if (aB && on_z_axis(xB, yB)) rotate_axis<Exact>(8, xB, yB, zB, oxB, oyB, ozB);
+            if (aA && on_z_axis(xA, yA)) {
+                rotate_axis<Exact>(8, xA, yA, zA, oxA, oyA, ozA);
+                oxA = -oxA;
+                oyA = -oyA;
+                ozA = -ozA;
+            }
+            if (aB && on_z_axis(xB, yB)) {
+                rotate_axis<Exact>(8, xB, yB, zB, oxB, oyB, ozB);
+                oxB = -oxB;
+                oyB = -oyB;
+                ozB = -ozB;
+            }
             nx = O::pk(oxA, oxB);
             ny = O::pk(oyA, oyB);
             nz = O::pk(ozA, ozB);
         }
-        zx = O::add(nx, px);
-        zy = O::add(ny, py);
-        zz = O::add(nz, pz);
+        zx = O::rsub(px, nx);  // rotate(z) + p
+        zy = O::rsub(py, ny);
+        zz = O::rsub(pz, nz);
     }
     float d0, d1;
     O::up(dr, d0, d1);
@@ -372,6 +406,63 @@ __device__ __forceinline__ float shape_de(const ShapeDev& s, float x, float y, f
     if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return polar_de(s, x, y, z);
     if (s.power == 8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
     return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
+}
+
+// FMA-contracted P=8 Mandelbulb (CG_NUMERICS_FAST).  Same polynomial as
+// rotate_p8 but regrouped for fused multiply-adds and approximate division
+// and square root; its loop state is not bit-identical to the reference.
+__device__ __forceinline__ float fast_sqrt(float x) {
+    return x > 0.0f ? x * rsqrtf(x) : 0.0f;
+}
+
+__device__ __forceinline__ float mandelbulb_p8_fast(uint32_t max_iters, float bailout, float px,
+                                                    float py, float pz) {
+    float zx = px, zy = py, zz = pz, dr = 1.0f, r = 0.0f;
+    for (uint32_t i = 0; i < max_iters; ++i) {
+        const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+        r = fast_sqrt(r2);
+        if (r > bailout) break;
+        const float rr2 = r * r, rr4 = rr2 * rr2;
+        dr = fmaf(rr4 * rr2 * r * 8.0f, dr, 1.0f);
+        const float x = zx, y = zy, z = zz;
+        const float x2 = x * x, y2 = y * y, z2 = z * z;
+        const float y4 = y2 * y2;
+        const float rxy2 = x2 + y2;
+        const float rxy4 = rxy2 * rxy2;
+        // num = z8 - 28 z6 rxy2 + 70 z4 rxy4 - 28 z2 rxy6 (Horner in z2)
+        const float num = fmaf(fmaf(fmaf(z2 - 28.0f * rxy2, z2, 70.0f * rxy4), z2,
+                                    -28.0f * rxy4 * rxy2), z2, 0.0f);
+        const float a = 1.0f + __fdividef(num, rxy4 * rxy4);
+        const float X = fmaf(fmaf(fmaf(x2 - 28.0f * y2, x2, 70.0f * y4), x2, -28.0f * y4 * y2),
+                             x2, -y4 * y4);
+        const float Y = fmaf(fmaf(x2 - 7.0f * y2, x2, 7.0f * y4), x2, -y4 * y2);
+        const float Z = fmaf(z2 - 6.0f * rxy2, z2, rxy4);
+        zx = fmaf(a, X, px);
+        zy = fmaf(8.0f * a * x * y, Y, py);
+        zz = fmaf(8.0f * z * fast_sqrt(rxy2) * (z2 - rxy2), Z, pz);
+    }
+    return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
+}
+
+// Kernel modes.
+enum Mode { MODE_P8 = 0, MODE_INT = 1, MODE_POLAR = 2, MODE_SPHERE = 3, MODE_P8_FAST = 4 };
+
+template <int M>
+__device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
+    if (M == MODE_P8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_POLAR) return polar_de(s, x, y, z);
+    if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
+    return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
+}
+
+
+// Kernel mode of a shape (integer P=8 takes the polynomial).
+__host__ __device__ __forceinline__ int mode_of(const ShapeDev& s, uint32_t numerics) {
+    if (s.kind == CG_SHAPE_SPHERE) return MODE_SPHERE;
+    if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return MODE_POLAR;
+    if (s.power == 8) return numerics == CG_NUMERICS_FAST ? MODE_P8_FAST : MODE_P8;
+    return MODE_INT;
 }
 
 }  // namespace cg

@@ -8,54 +8,6 @@
 
 namespace cg {
 
-// FMA-contracted P=8 Mandelbulb (CG_NUMERICS_FAST).  Same polynomial as
-// rotate_p8 but regrouped for fused multiply-adds and approximate division
-// and square root; its loop state is not bit-identical to the reference.
-__device__ __forceinline__ float fast_sqrt(float x) {
-    return x > 0.0f ? x * rsqrtf(x) : 0.0f;
-}
-
-__device__ __forceinline__ float mandelbulb_p8_fast(uint32_t max_iters, float bailout, float px,
-                                                    float py, float pz) {
-    float zx = px, zy = py, zz = pz, dr = 1.0f, r = 0.0f;
-    for (uint32_t i = 0; i < max_iters; ++i) {
-        const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
-        r = fast_sqrt(r2);
-        if (r > bailout) break;
-        const float rr2 = r * r, rr4 = rr2 * rr2;
-        dr = fmaf(rr4 * rr2 * r * 8.0f, dr, 1.0f);
-        const float x = zx, y = zy, z = zz;
-        const float x2 = x * x, y2 = y * y, z2 = z * z;
-        const float y4 = y2 * y2;
-        const float rxy2 = x2 + y2;
-        const float rxy4 = rxy2 * rxy2;
-        // num = z8 - 28 z6 rxy2 + 70 z4 rxy4 - 28 z2 rxy6 (Horner in z2)
-        const float num = fmaf(fmaf(fmaf(z2 - 28.0f * rxy2, z2, 70.0f * rxy4), z2,
-                                    -28.0f * rxy4 * rxy2), z2, 0.0f);
-        const float a = 1.0f + __fdividef(num, rxy4 * rxy4);
-        const float X = fmaf(fmaf(fmaf(x2 - 28.0f * y2, x2, 70.0f * y4), x2, -28.0f * y4 * y2),
-                             x2, -y4 * y4);
-        const float Y = fmaf(fmaf(x2 - 7.0f * y2, x2, 7.0f * y4), x2, -y4 * y2);
-        const float Z = fmaf(z2 - 6.0f * rxy2, z2, rxy4);
-        zx = fmaf(a, X, px);
-        zy = fmaf(8.0f * a * x * y, Y, py);
-        zz = fmaf(8.0f * z * fast_sqrt(rxy2) * (z2 - rxy2), Z, pz);
-    }
-    return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
-}
-
-// Kernel modes.
-enum Mode { MODE_P8 = 0, MODE_INT = 1, MODE_POLAR = 2, MODE_SPHERE = 3, MODE_P8_FAST = 4 };
-
-template <int M>
-__device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
-    if (M == MODE_P8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
-    if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
-    if (M == MODE_POLAR) return polar_de(s, x, y, z);
-    if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
-    return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
-}
-
 template <int M>
 __global__ void __launch_bounds__(256) k_de_points(ShapeDev s, const float* __restrict__ pts,
                                                    uint64_t n, float* __restrict__ out) {
@@ -235,12 +187,6 @@ cg_status launch_grid_work(const ShapeDev& s, const GridDev& g, unsigned long lo
     return CG_OK;
 }
 
-static int mode_of(const ShapeDev& s, uint32_t numerics) {
-    if (s.kind == CG_SHAPE_SPHERE) return MODE_SPHERE;
-    if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return MODE_POLAR;
-    if (s.power == 8) return numerics == CG_NUMERICS_FAST ? MODE_P8_FAST : MODE_P8;
-    return MODE_INT;
-}
 
 cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
                            uint32_t numerics, cudaStream_t st) {

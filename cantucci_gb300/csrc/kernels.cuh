@@ -30,6 +30,9 @@ GridDev make_grid(const SpanSetup& su, uint32_t res);
 
 cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, float* out,
                            uint32_t numerics, cudaStream_t st);
+// Batched-mesher knobs: "batch_chunk", "batch_block", "batch_brick_min_res".
+int set_batch_option(const char* name, int64_t v);
+
 // Step-1 kernel variants (cg_set_option "de_grid_kernel").
 enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3 };
 int set_de_grid_kernel(int v);

@@ -1,0 +1,543 @@
+// mesh_batch.cu -- many octree spans meshed together: the GPU form of
+// ShapeMesh::update's thread pool, which runs one generate_for_box job per
+// empty leaf (src/mesh/mod.rs:129-161).
+//
+// Every span of a batch keeps its own arrays (same layout as one span,
+// mesh_rows.cuh) at offsets given by a span table, so each span's mesh is
+// exactly what generate_for_box gives for it alone.
+//
+//   step 1   one persistent kernel; warps take chunks of work items from an
+//            atomic queue.  An item is a 2x4x4 brick of corners (spans with
+//            res >= 32) or 32 consecutive corners in GridTable order (smaller
+//            spans, where bricks would leave lanes idle).
+//   step 2/3 grid-stride kernels over the cell rows of all spans; one
+//            exclusive scan over all rows gives every span's vertex range
+//            (and, for quads, its index range) in span order.
+// No launch depends on a host-side count, so a batch is captured into one
+// CUDA graph and replayed.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "mesh_rows.cuh"
+
+namespace cg {
+
+struct BatchJob {
+    float start[3], across[3];  // widened span (buffer.rs:64-67,77)
+    float inv_res;
+    PlaceParams pp;             // start, step, FD delta
+    MeshDims d;
+    uint64_t dist_off;          // floats into dists
+    uint64_t sgn_off;           // words into sgn
+    uint64_t cw_off;            // words into cellbits / wordoff
+    uint32_t row_begin;         // first global cell row
+    uint32_t item_begin;        // first global step-1 work item
+    uint32_t items;
+    uint32_t brick;             // 1: 2x4x4 bricks, 0: 32 consecutive corners
+};
+
+struct BatchTotals {
+    uint32_t vertices, quads, status, queue;
+};
+
+// Tuning knobs (cg_set_option "batch_chunk", "batch_block", "batch_brick_min_res").
+static uint32_t g_batch_chunk = 64;
+static uint32_t g_batch_block = 256;
+static uint32_t g_batch_brick_min_res = 32;
+
+int set_batch_option(const char* name, int64_t v) {
+    if (!strcmp(name, "batch_chunk") && v >= 1 && v <= 4096) {
+        g_batch_chunk = (uint32_t)v;
+        return 1;
+    }
+    if (!strcmp(name, "batch_block") && (v == 64 || v == 128 || v == 256 || v == 512)) {
+        g_batch_block = (uint32_t)v;
+        return 1;
+    }
+    if (!strcmp(name, "batch_brick_min_res") && v >= 2 && v <= 2048) {
+        g_batch_brick_min_res = (uint32_t)v;
+        return 1;
+    }
+    return 0;
+}
+
+// Index of the last entry of a non-decreasing table with key <= v.
+__device__ __forceinline__ uint32_t find_job(const BatchJob* __restrict__ jobs, uint32_t njobs,
+                                             uint32_t v, bool by_item) {
+    uint32_t lo = 0, hi = njobs;  // answer in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t key = by_item ? jobs[mid].item_begin : jobs[mid].row_begin;
+        if (key <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float job_coord(const BatchJob& j, int k, uint32_t v) {
+    return __fadd_rn(j.start[k], __fmul_rn(j.across[k], __fmul_rn((float)v, j.inv_res)));
+}
+
+// Step 1 over all spans: persistent warps pull chunks of items from `queue`.
+template <int M>
+__global__ void k_batch_de(ShapeDev s, const BatchJob* __restrict__ jobs, uint32_t njobs,
+                           uint32_t total_items, uint32_t chunk, BatchTotals* __restrict__ tot,
+                           float* __restrict__ dists, uint32_t* __restrict__ sgn) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&tot->queue, chunk);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= total_items) break;
+        const uint32_t end = min(base + chunk, total_items);
+        uint32_t j = find_job(jobs, njobs, base, true);
+        for (uint32_t item = base; item < end; ++item) {
+            while (j + 1 < njobs && jobs[j + 1].item_begin <= item) ++j;
+            const BatchJob& J = jobs[j];
+            const uint32_t n = J.d.n, W = J.d.W;
+            float* out = dists + J.dist_off;
+            uint32_t* sg = sgn + J.sgn_off;
+            const uint32_t local = item - J.item_begin;
+            if (J.brick) {
+                const uint32_t BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
+                const uint32_t bz = local % BZ, t = local / BZ, by = t % BY, bx = t / BY;
+                const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
+                const uint32_t x = 2 * bx + dx, y = 4 * by + dy, z = 4 * bz + dz;
+                uint32_t bit = 0;
+                if (x < n && y < n && z < n) {
+                    const float d = eval<M>(s, job_coord(J, 0, x), job_coord(J, 1, y),
+                                            job_coord(J, 2, z));
+                    out[((size_t)x * n + y) * n + z] = d;
+                    bit = (__float_as_uint(d) >> 31) ? 0u : (1u << (z & 31));
+                }
+                bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 1);
+                bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 2);
+                if (dz == 0 && bit) atomicOr(&sg[(x * n + y) * W + (z >> 5)], bit);
+            } else {
+                const uint32_t i = local * 32 + lane;
+                if (i < n * n * n) {
+                    const uint32_t z = i % n, row = i / n, y = row % n, x = row / n;
+                    const float d = eval<M>(s, job_coord(J, 0, x), job_coord(J, 1, y),
+                                            job_coord(J, 2, z));
+                    out[i] = d;
+                    if (!(__float_as_uint(d) >> 31)) atomicOr(&sg[row * W + (z >> 5)], 1u << (z & 31));
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_batch_cells(const BatchJob* __restrict__ jobs, uint32_t njobs, uint32_t rows,
+                              const uint32_t* __restrict__ sgn, uint32_t* __restrict__ cellbits,
+                              uint32_t* __restrict__ wordoff, uint32_t* __restrict__ rowcnt) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const BatchJob& J = jobs[find_job(jobs, njobs, r, false)];
+        rowcnt[r] = cells_row(sgn + J.sgn_off, J.d, r - J.row_begin, cellbits + J.cw_off,
+                              wordoff + J.cw_off);
+    }
+}
+
+__global__ void k_batch_vertex_list(const BatchJob* __restrict__ jobs, uint32_t njobs,
+                                    uint32_t rows, const uint32_t* __restrict__ cellbits,
+                                    const uint32_t* __restrict__ wordoff,
+                                    const uint32_t* __restrict__ rowoff, uint64_t vcap,
+                                    uint32_t* __restrict__ cellidx,
+                                    uint32_t* __restrict__ celljob) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const uint32_t j = find_job(jobs, njobs, r, false);
+        const BatchJob& J = jobs[j];
+        // Vertex ids at or past the capacity are not listed (and not placed);
+        // the totals still report the full count.
+        vertex_list_row(J.d, r - J.row_begin, cellbits + J.cw_off, wordoff + J.cw_off, rowoff[r],
+                        vcap, cellidx, celljob, j);
+    }
+}
+
+template <int M>
+__global__ void __launch_bounds__(128) k_batch_place(ShapeDev s, const BatchJob* __restrict__ jobs,
+                                                     const float* __restrict__ dists,
+                                                     const uint32_t* __restrict__ cellidx,
+                                                     const uint32_t* __restrict__ celljob,
+                                                     BatchTotals* __restrict__ tot,
+                                                     cg_vertex* __restrict__ verts, uint64_t vcap) {
+    const uint32_t V = (uint32_t)min((uint64_t)tot->vertices, vcap);
+    bool bad = false;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const BatchJob& J = jobs[celljob[v]];
+        bad |= !place_vertex<M>(s, J.pp, J.d, dists + J.dist_off, cellidx[v],
+                                reinterpret_cast<float*>(verts + v));
+    }
+    if (bad) atomicOr(&tot->status, MESH_LERP_FAIL);
+}
+
+__global__ void k_batch_quad_count(const BatchJob* __restrict__ jobs, uint32_t njobs,
+                                   uint32_t rows, const uint32_t* __restrict__ sgn,
+                                   uint32_t* __restrict__ quadcnt) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const BatchJob& J = jobs[find_job(jobs, njobs, r, false)];
+        quadcnt[r] = quad_count_row(sgn + J.sgn_off, J.d, r - J.row_begin);
+    }
+}
+
+__global__ void k_batch_quad_emit(const BatchJob* __restrict__ jobs, uint32_t njobs,
+                                  uint32_t rows, const uint32_t* __restrict__ sgn,
+                                  const float* __restrict__ dists,
+                                  const uint32_t* __restrict__ cellbits,
+                                  const uint32_t* __restrict__ wordoff,
+                                  const uint32_t* __restrict__ rowoff,
+                                  const uint32_t* __restrict__ quadoff, uint32_t* __restrict__ idx,
+                                  uint64_t icap) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const BatchJob& J = jobs[find_job(jobs, njobs, r, false)];
+        const uint32_t* ro = rowoff + J.row_begin;
+        quad_emit_row(sgn + J.sgn_off, J.d, dists + J.dist_off, cellbits + J.cw_off,
+                      wordoff + J.cw_off, ro, ro[0], quadoff[r], idx, icap, r - J.row_begin);
+    }
+}
+
+// Per-span vertex and index ranges.
+__global__ void k_batch_results(const BatchJob* __restrict__ jobs, uint32_t njobs,
+                                const uint32_t* __restrict__ rowoff,
+                                const uint32_t* __restrict__ quadoff,
+                                const BatchTotals* __restrict__ tot,
+                                cg_job_mesh* __restrict__ out) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < njobs;
+         j += gridDim.x * blockDim.x) {
+        const uint32_t r0 = jobs[j].row_begin;
+        const bool last = j + 1 == njobs;
+        const uint32_t v0 = rowoff[r0], q0 = quadoff[r0];
+        const uint32_t v1 = last ? tot->vertices : rowoff[jobs[j + 1].row_begin];
+        const uint32_t q1 = last ? tot->quads : quadoff[jobs[j + 1].row_begin];
+        cg_job_mesh m;
+        m.vertex_offset = v0;
+        m.index_offset = 6ull * q0;
+        m.vertices = v1 - v0;
+        m.indices = 6u * (q1 - q0);
+        out[j] = m;
+    }
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+struct cg_batch {
+    int device = 0;
+    uint32_t njobs = 0;
+    uint32_t total_items = 0;
+    uint32_t rows = 0;
+    uint64_t vertex_cap = 0;
+    char* work = nullptr;
+    BatchJob* jobs = nullptr;  // device
+    float* dists = nullptr;
+    uint32_t *sgn = nullptr, *cellbits = nullptr, *wordoff = nullptr;
+    uint32_t *rowcnt = nullptr, *rowoff = nullptr, *quadcnt = nullptr, *quadoff = nullptr;
+    uint32_t *cellidx = nullptr, *celljob = nullptr, *scratch = nullptr;
+    BatchTotals* tot = nullptr;
+    size_t sgn_words = 0;
+    std::vector<uint32_t> res;  // per job, host copy
+    // graph cache
+    cudaGraphExec_t exec = nullptr;
+    unsigned char graph_key[160] = {0};
+    std::mutex mu;
+};
+
+namespace {
+
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" {
+
+cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_jobs,
+                          uint64_t vertex_cap, cg_batch** out) {
+    if (!out || (!host_jobs && n_jobs) || n_jobs == 0) {
+        set_error("bad arguments to cg_batch_create");
+        return CG_EINVAL;
+    }
+    *out = nullptr;
+    std::vector<BatchJob> jobs(n_jobs);
+    uint64_t dist = 0, sgnw = 0, cw = 0, rows = 0, items = 0;
+    for (uint32_t i = 0; i < n_jobs; ++i) {
+        const cg_span_job& hj = host_jobs[i];
+        const uint32_t res = hj.resolution;
+        for (int k = 0; k < 3; ++k) {
+            if (!(hj.span.start[k] < hj.span.end[k])) {
+                set_error("job %u: span.start[%d] < span.end[%d] does not hold", i, k, k);
+                return CG_EINVAL;
+            }
+        }
+        if (res < 2 || (res & (res - 1)) || res > 1024) {
+            set_error("job %u: resolution %u must be a power of two in [2, 1024]", i, res);
+            return CG_EINVAL;
+        }
+        const SpanSetup su = setup_span(hj.span, res);
+        BatchJob& J = jobs[i];
+        memset(&J, 0, sizeof J);
+        for (int k = 0; k < 3; ++k) {
+            J.start[k] = su.start[k];
+            J.across[k] = su.across[k];
+        }
+        J.inv_res = 1.0f / (float)res;
+        J.pp = place_params(su);
+        J.d = mesh_dims(res);
+        const uint64_t n = J.d.n;
+        J.dist_off = dist;
+        J.sgn_off = sgnw;
+        J.cw_off = cw;
+        J.row_begin = (uint32_t)rows;
+        J.item_begin = (uint32_t)items;
+        J.brick = res >= g_batch_brick_min_res ? 1u : 0u;
+        J.items = J.brick ? (uint32_t)(((n + 1) >> 1) * ((n + 3) >> 2) * ((n + 3) >> 2))
+                          : (uint32_t)((n * n * n + 31) / 32);
+        dist += n * n * n;
+        sgnw += n * n * J.d.W;
+        cw += (uint64_t)res * res * J.d.Wc;
+        rows += (uint64_t)res * res;
+        items += J.items;
+        if (rows > (16u << 20) || items > 0x7FFFFFFFu || dist > 0xFFFFFFFFull * 4) {
+            set_error("batch too large: %llu cell rows", (unsigned long long)rows);
+            return CG_EINVAL;
+        }
+    }
+    cg_batch* b = new (std::nothrow) cg_batch();
+    if (!b) return CG_ENOMEM;
+    b->device = device;
+    b->njobs = n_jobs;
+    b->total_items = (uint32_t)items;
+    b->rows = (uint32_t)rows;
+    b->vertex_cap = vertex_cap;
+    b->sgn_words = sgnw;
+    b->res.resize(n_jobs);
+    for (uint32_t i = 0; i < n_jobs; ++i) b->res[i] = host_jobs[i].resolution;
+    size_t off = 0;
+    std::vector<std::pair<void**, size_t>> parts = {
+        {(void**)&b->jobs, sizeof(BatchJob) * n_jobs},
+        {(void**)&b->dists, dist * 4},
+        {(void**)&b->sgn, sgnw * 4},
+        {(void**)&b->cellbits, cw * 4},
+        {(void**)&b->wordoff, cw * 4},
+        {(void**)&b->rowcnt, rows * 4},
+        {(void**)&b->rowoff, rows * 4},
+        {(void**)&b->quadcnt, rows * 4},
+        {(void**)&b->quadoff, rows * 4},
+        {(void**)&b->cellidx, (vertex_cap ? vertex_cap : 1) * 4},
+        {(void**)&b->celljob, (vertex_cap ? vertex_cap : 1) * 4},
+        {(void**)&b->scratch, scan_scratch_words((uint32_t)rows) * 4},
+        {(void**)&b->tot, sizeof(BatchTotals)},
+    };
+    for (auto& p : parts) off += al(p.second);
+    DeviceScope g(device);
+    cg_status st = cuda_status(cudaMalloc(&b->work, off), "cudaMalloc", __FILE__, __LINE__);
+    if (st != CG_OK) {
+        delete b;
+        return st;
+    }
+    off = 0;
+    for (auto& p : parts) {
+        *p.first = b->work + off;
+        off += al(p.second);
+    }
+    st = cuda_status(cudaMemcpy(b->jobs, jobs.data(), sizeof(BatchJob) * n_jobs,
+                                cudaMemcpyHostToDevice),
+                     "cudaMemcpy", __FILE__, __LINE__);
+    if (st != CG_OK) {
+        cudaFree(b->work);
+        delete b;
+        return st;
+    }
+    *out = b;
+    return CG_OK;
+}
+
+void cg_batch_destroy(cg_batch* b) {
+    if (!b) return;
+    DeviceScope g(b->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->work) cudaFree(b->work);
+    delete b;
+}
+
+cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
+                        uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                        cg_job_mesh* results, uint32_t* totals, void* stream) {
+    if (!b || !shape || !results || !totals || (vertex_cap && !vertices) ||
+        (index_cap && !indices)) {
+        set_error("bad arguments to cg_batch_mesh");
+        return CG_EINVAL;
+    }
+    if (vertex_cap > b->vertex_cap) vertex_cap = b->vertex_cap;
+    if (shape->kind == CG_SHAPE_MANDELBULB && (shape->power < 0 || shape->power > 255 ||
+                                                shape->max_iters < 1)) {
+        set_error("bad Mandelbulb parameters");
+        return CG_EINVAL;
+    }
+    const ShapeDev s = make_shape_dev(*shape);
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned B = g_batch_block;
+    CG_CUDA(cudaMemsetAsync(b->tot, 0, sizeof(BatchTotals), st));
+    CG_CUDA(cudaMemsetAsync(b->sgn, 0, b->sgn_words * 4, st));
+    {
+        const unsigned G = (unsigned)sm_count() * (2048 / B);
+        const uint32_t chunk = g_batch_chunk;
+        switch (mode_of(s, CG_NUMERICS_EXACT)) {
+        case MODE_P8:
+            k_batch_de<MODE_P8><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk, b->tot,
+                                                 b->dists, b->sgn);
+            break;
+        case MODE_INT:
+            k_batch_de<MODE_INT><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
+                                                  b->tot, b->dists, b->sgn);
+            break;
+        case MODE_POLAR:
+            k_batch_de<MODE_POLAR><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
+                                                    b->tot, b->dists, b->sgn);
+            break;
+        default:
+            k_batch_de<MODE_SPHERE><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
+                                                     b->tot, b->dists, b->sgn);
+            break;
+        }
+        CG_CHECK_LAUNCH("k_batch_de");
+    }
+    const unsigned G = grid_for(b->rows, 256, 8);
+    k_batch_cells<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->cellbits, b->wordoff,
+                                     b->rowcnt);
+    CG_CHECK_LAUNCH("k_batch_cells");
+    CG_TRY(launch_exclusive_scan(b->rowcnt, b->rowoff, b->rows, b->scratch, &b->tot->vertices, st));
+    k_batch_vertex_list<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->cellbits, b->wordoff,
+                                           b->rowoff, vertex_cap, b->cellidx, b->celljob);
+    CG_CHECK_LAUNCH("k_batch_vertex_list");
+    {
+        const unsigned GP = (unsigned)sm_count() * 16;
+        switch (mode_of(s, CG_NUMERICS_EXACT)) {
+        case MODE_P8:
+            k_batch_place<MODE_P8><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
+                                                       b->celljob, b->tot, vertices, vertex_cap);
+            break;
+        case MODE_INT:
+            k_batch_place<MODE_INT><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
+                                                        b->celljob, b->tot, vertices, vertex_cap);
+            break;
+        case MODE_POLAR:
+            k_batch_place<MODE_POLAR><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
+                                                          b->celljob, b->tot, vertices, vertex_cap);
+            break;
+        default:
+            k_batch_place<MODE_SPHERE><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
+                                                           b->celljob, b->tot, vertices,
+                                                           vertex_cap);
+            break;
+        }
+        CG_CHECK_LAUNCH("k_batch_place");
+    }
+    k_batch_quad_count<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->quadcnt);
+    CG_CHECK_LAUNCH("k_batch_quad_count");
+    CG_TRY(launch_exclusive_scan(b->quadcnt, b->quadoff, b->rows, b->scratch, &b->tot->quads, st));
+    k_batch_quad_emit<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->dists, b->cellbits,
+                                         b->wordoff, b->rowoff, b->quadoff, indices, index_cap);
+    CG_CHECK_LAUNCH("k_batch_quad_emit");
+    k_batch_results<<<grid_for(b->njobs, 256, 4), 256, 0, st>>>(b->jobs, b->njobs, b->rowoff,
+                                                                 b->quadoff, b->tot, results);
+    CG_CHECK_LAUNCH("k_batch_results");
+    CG_CUDA(cudaMemcpyAsync(totals, b->tot, 3 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    return CG_OK;
+}
+
+cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
+                              uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                              cg_job_mesh* results, uint32_t* totals, void* stream) {
+    if (!b || !shape) {
+        set_error("bad arguments to cg_batch_mesh_graph");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceScope g(b->device);
+    // The graph bakes in every argument and the tuning knobs: recapture when
+    // any of them changes.
+    unsigned char key[160];
+    memset(key, 0, sizeof key);
+    size_t o = 0;
+    auto put = [&](const void* p, size_t n) {
+        memcpy(key + o, p, n);
+        o += n;
+    };
+    put(shape, sizeof(cg_shape));
+    put(&vertices, sizeof vertices);
+    put(&vertex_cap, 8);
+    put(&indices, sizeof indices);
+    put(&index_cap, 8);
+    put(&results, sizeof results);
+    put(&totals, sizeof totals);
+    put(&g_batch_chunk, 4);
+    put(&g_batch_block, 4);
+    put(&g_batch_brick_min_res, 4);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!b->exec || memcmp(key, b->graph_key, sizeof key) != 0) {
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        cudaStream_t cap = nullptr;
+        CG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cg_status rs = cuda_status(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal),
+                                   "cudaStreamBeginCapture", __FILE__, __LINE__);
+        if (rs == CG_OK) {
+            rs = cg_batch_mesh(b, shape, vertices, vertex_cap, indices, index_cap, results, totals,
+                               cap);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(cap, &graph);
+            if (rs == CG_OK) rs = cuda_status(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+            if (rs == CG_OK)
+                rs = cuda_status(cudaGraphInstantiate(&b->exec, graph, 0), "cudaGraphInstantiate",
+                                 __FILE__, __LINE__);
+            if (graph) cudaGraphDestroy(graph);
+        }
+        cudaStreamDestroy(cap);
+        if (rs != CG_OK) {
+            b->exec = nullptr;
+            return rs;
+        }
+        memcpy(b->graph_key, key, sizeof key);
+    }
+    CG_CUDA(cudaGraphLaunch(b->exec, st));
+    return CG_OK;
+}
+
+cg_status cg_batch_dists(cg_batch* b, uint32_t job, const float** dists) {
+    if (!b || job >= b->njobs || !dists) {
+        set_error("bad arguments to cg_batch_dists");
+        return CG_EINVAL;
+    }
+    uint64_t off = 0;
+    for (uint32_t i = 0; i < job; ++i) {
+        const uint64_t n = b->res[i] + 1;
+        off += n * n * n;
+    }
+    *dists = b->dists + off;
+    return CG_OK;
+}
+
+}  // extern "C"

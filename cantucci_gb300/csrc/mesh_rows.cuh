@@ -1,0 +1,289 @@
+// mesh_rows.cuh -- the per-row and per-vertex bodies of naive surface nets
+// (MeshBuffer::naive_surface_nets, src/mesh/buffer.rs:85-372), shared by the
+// single-span kernels (mesh.cu) and the batched multi-span kernels
+// (mesh_batch.cu).  All pointers are already offset to one span's arrays.
+//
+// Layout per span (res cells per axis, n = res + 1 corners per axis):
+//   dists    f32 [n][n][n]     x-major, z fastest (GridTable, src/util/grid.rs:45-48)
+//   sgn      u32 [n][n][W]     W = ceil(n/32); bit b of word w = is_sign_positive(dists[x][y][32w+b])
+//   cellbits u32 [res][res][Wc] Wc = ceil(res/32); bit = cell (x, y, 32w+b) crosses the surface
+//   wordoff  u32 [res][res][Wc] surface cells of the row before word w
+//   rowoff   u32 [res*res]     vertices before cell row (x, y) (exclusive scan)
+// A vertex id is rowoff[x,y] + wordoff[x,y,w] + popc(cellbits[x,y,w] & below(b)):
+// the running count of surface cells in cube() order that the reference
+// assigns with vertices.len() - 1 (buffer.rs:274).
+#pragma once
+
+#include <cstdint>
+
+#include "de.cuh"
+#include "kernels.cuh"
+
+namespace cg {
+
+__device__ __forceinline__ uint32_t valid_mask(uint32_t res, uint32_t w) {
+    const uint32_t lo = w * 32;
+    return (lo + 32 <= res) ? 0xFFFFFFFFu : ((1u << (res - lo)) - 1u);
+}
+
+// Sign word of corner row `row` shifted by one corner: bit b = corner 32w+b+1.
+__device__ __forceinline__ uint32_t sign_hi(const uint32_t* __restrict__ sgn, uint32_t row,
+                                            uint32_t W, uint32_t w) {
+    const uint32_t lo = sgn[row * W + w];
+    const uint32_t nx = (w + 1 < W) ? sgn[row * W + w + 1] : 0u;
+    return (lo >> 1) | (nx << 31);
+}
+
+// Surface cells of cell row r = (x, y) (buffer.rs:116-147): a cell crosses
+// iff the sign bits of its 8 corners are not all equal.  Returns the count.
+__device__ __forceinline__ uint32_t cells_row(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                              uint32_t r, uint32_t* __restrict__ cellbits,
+                                              uint32_t* __restrict__ wordoff) {
+    const uint32_t x = r / d.res, y = r % d.res;
+    const uint32_t r00 = x * d.n + y, r01 = r00 + 1, r10 = r00 + d.n, r11 = r10 + 1;
+    uint32_t run = 0;
+    for (uint32_t w = 0; w < d.Wc; ++w) {
+        const uint32_t a0 = sgn[r00 * d.W + w], a1 = sgn[r01 * d.W + w];
+        const uint32_t a2 = sgn[r10 * d.W + w], a3 = sgn[r11 * d.W + w];
+        const uint32_t b0 = sign_hi(sgn, r00, d.W, w), b1 = sign_hi(sgn, r01, d.W, w);
+        const uint32_t b2 = sign_hi(sgn, r10, d.W, w), b3 = sign_hi(sgn, r11, d.W, w);
+        const uint32_t all1 = a0 & a1 & a2 & a3 & b0 & b1 & b2 & b3;
+        const uint32_t any1 = a0 | a1 | a2 | a3 | b0 | b1 | b2 | b3;
+        const uint32_t surf = any1 & ~all1 & valid_mask(d.res, w);
+        cellbits[r * d.Wc + w] = surf;
+        wordoff[r * d.Wc + w] = run;
+        run += __popc(surf);
+    }
+    return run;
+}
+
+// Cell index (within its span) of every vertex of cell row r, written at the
+// row's vertex ids starting from `base` (only ids below `cap`); `tag` (if
+// any) receives `tag_value` at the same ids.
+__device__ __forceinline__ void vertex_list_row(const MeshDims& d, uint32_t r,
+                                                const uint32_t* __restrict__ cellbits,
+                                                const uint32_t* __restrict__ wordoff, uint32_t base,
+                                                uint64_t cap, uint32_t* __restrict__ cellidx,
+                                                uint32_t* __restrict__ tag, uint32_t tag_value) {
+    for (uint32_t w = 0; w < d.Wc; ++w) {
+        uint32_t bits = cellbits[r * d.Wc + w];
+        uint32_t v = base + wordoff[r * d.Wc + w];
+        while (bits) {
+            const uint32_t b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (v < cap) {
+                cellidx[v] = r * d.res + w * 32 + b;
+                if (tag) tag[v] = tag_value;
+            }
+            ++v;
+        }
+    }
+}
+
+struct PlaceParams {
+    float start[3], step[3], delta[3];
+};
+
+PlaceParams place_params(const SpanSetup& su);
+
+// Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
+// crossings, DE at the vertex and the six-sample central-difference normal.
+// Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
+template <int M>
+__device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
+                                             const MeshDims& d, const float* __restrict__ dists,
+                                             uint32_t c, float* __restrict__ o) {
+    const uint32_t z = c % d.res, xy = c / d.res, y = xy % d.res, x = xy / d.res;
+    float dd[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t cx = x + ((k >> 2) & 1), cy = y + ((k >> 1) & 1), cz = z + (k & 1);
+        dd[k] = dists[((size_t)cx * d.n + cy) * d.n + cz];
+    }
+    const float p0x = __fadd_rn(pp.start[0], __fmul_rn((float)x, pp.step[0]));
+    const float p0y = __fadd_rn(pp.start[1], __fmul_rn((float)y, pp.step[1]));
+    const float p0z = __fadd_rn(pp.start[2], __fmul_rn((float)z, pp.step[2]));
+    // EDGES (buffer.rs:155-176): x edges, y edges, z edges.
+    const uint8_t EF[12] = {0, 1, 2, 3, 0, 1, 4, 5, 0, 2, 4, 6};
+    const uint8_t ET[12] = {4, 5, 6, 7, 2, 3, 6, 7, 1, 3, 5, 7};
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+    uint32_t count = 0;
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        const int from = EF[k], to = ET[k];
+        const float df0 = dd[from], dt0 = dd[to];
+        if ((__float_as_uint(df0) >> 31) == (__float_as_uint(dt0) >> 31)) continue;
+        float df, dt;
+        if (df0 < 0.0f) {
+            df = df0;
+            dt = dt0;
+        } else {
+            df = -df0;
+            dt = -dt0;
+        }
+        float wgt;
+        if (dt == df) {
+            wgt = 0.5f;
+        } else {
+            const float delta = __fsub_rn(dt, df);
+            wgt = __fdiv_rn(__fadd_rn(df, delta), delta);
+        }
+        // math::lerp asserts 0 <= t <= 1 (src/math.rs:19).
+        if (!(wgt >= 0.0f && wgt <= 1.0f)) {
+            bad = true;
+            wgt = 0.0f;
+        }
+        const float ax = __fadd_rn(p0x, ((from >> 2) & 1) ? pp.step[0] : 0.0f);
+        const float ay = __fadd_rn(p0y, ((from >> 1) & 1) ? pp.step[1] : 0.0f);
+        const float az = __fadd_rn(p0z, (from & 1) ? pp.step[2] : 0.0f);
+        const float bx = __fadd_rn(p0x, ((to >> 2) & 1) ? pp.step[0] : 0.0f);
+        const float by = __fadd_rn(p0y, ((to >> 1) & 1) ? pp.step[1] : 0.0f);
+        const float bz = __fadd_rn(p0z, (to & 1) ? pp.step[2] : 0.0f);
+        // Point3::lerp: self * (1 - t) + other * t (src/math.rs:45-49).
+        const float omt = __fsub_rn(1.0f, wgt);
+        sx = __fadd_rn(sx, __fadd_rn(__fmul_rn(ax, omt), __fmul_rn(bx, wgt)));
+        sy = __fadd_rn(sy, __fadd_rn(__fmul_rn(ay, omt), __fmul_rn(by, wgt)));
+        sz = __fadd_rn(sz, __fadd_rn(__fmul_rn(az, omt), __fmul_rn(bz, wgt)));
+        ++count;
+    }
+    const float cf = (float)count;
+    const float vx = __fadd_rn(0.0f, __fdiv_rn(sx, cf));
+    const float vy = __fadd_rn(0.0f, __fdiv_rn(sy, cf));
+    const float vz = __fadd_rn(0.0f, __fdiv_rn(sz, cf));
+    // Sample 0 is the vertex; samples 1..6 are p + unit * (+-delta) along
+    // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
+    // loop is kept rolled so that one copy of the estimator is in the code.
+    float de[7];
+#pragma unroll 1
+    for (int k = 0; k < 7; ++k) {
+        float qx = vx, qy = vy, qz = vz;
+        if (k > 0) {
+            const int axis = (k - 1) >> 1;
+            const bool neg = ((k - 1) & 1) != 0;
+            const float zero = neg ? -0.0f : 0.0f;
+            const float dd0 = axis == 0 ? pp.delta[0] : (axis == 1 ? pp.delta[1] : pp.delta[2]);
+            const float off = neg ? -dd0 : dd0;
+            qx = __fadd_rn(vx, axis == 0 ? off : zero);
+            qy = __fadd_rn(vy, axis == 1 ? off : zero);
+            qz = __fadd_rn(vz, axis == 2 ? off : zero);
+        }
+        const float val = eval<M>(s, qx, qy, qz);
+#pragma unroll
+        for (int j = 0; j < 7; ++j) de[j] = (j == k) ? val : de[j];
+    }
+    const float nx = __fsub_rn(de[1], de[2]);
+    const float ny = __fsub_rn(de[3], de[4]);
+    const float nz = __fsub_rn(de[5], de[6]);
+    // cgmath normalize: v * (1 / |v|), |v| = sqrt((x*x + y*y) + z*z).
+    const float inv = __fdiv_rn(1.0f, magnitude<Exact>(nx, ny, nz));
+    if (o) {
+        o[0] = vx;
+        o[1] = vy;
+        o[2] = vz;
+        o[3] = __fmul_rn(nx, inv);
+        o[4] = __fmul_rn(ny, inv);
+        o[5] = __fmul_rn(nz, inv);
+        o[6] = de[0];
+    }
+    return !bad;
+}
+
+// Edge crossings of the corners of one corner row, 32 corners per word
+// (buffer.rs:299-371): bit b of ex/ey/ez = the +x/+y/+z edge of corner
+// (x, y, 32w+b) emits a quad.
+struct EdgeWords {
+    uint32_t ex, ey, ez;
+};
+
+__device__ __forceinline__ EdgeWords edge_words(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                                uint32_t x, uint32_t y, uint32_t w) {
+    const uint32_t r = x * d.n + y;
+    const uint32_t base = sgn[r * d.W + w];
+    const uint32_t valid = valid_mask(d.res, w);
+    const uint32_t zpos = valid & (w == 0 ? ~1u : ~0u);
+    EdgeWords e;
+    e.ex = (y > 0) ? ((base ^ sgn[(r + d.n) * d.W + w]) & zpos) : 0u;
+    e.ey = (x > 0) ? ((base ^ sgn[(r + 1) * d.W + w]) & zpos) : 0u;
+    e.ez = (x > 0 && y > 0) ? ((base ^ sign_hi(sgn, r, d.W, w)) & valid) : 0u;
+    return e;
+}
+
+__device__ __forceinline__ uint32_t quad_count_row(const uint32_t* __restrict__ sgn,
+                                                   const MeshDims& d, uint32_t r) {
+    const uint32_t x = r / d.res, y = r % d.res;
+    uint32_t c = 0;
+    for (uint32_t w = 0; w < d.Wc; ++w) {
+        const EdgeWords e = edge_words(sgn, d, x, y, w);
+        c += __popc(e.ex) + __popc(e.ey) + __popc(e.ez);
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint32_t vertex_id(const MeshDims& d, const uint32_t* __restrict__ cellbits,
+                                              const uint32_t* __restrict__ wordoff,
+                                              const uint32_t* __restrict__ rowoff, uint32_t x,
+                                              uint32_t y, uint32_t z) {
+    const uint32_t r = x * d.res + y, w = z >> 5, b = z & 31;
+    return rowoff[r] + wordoff[r * d.Wc + w] + __popc(cellbits[r * d.Wc + w] & ((1u << b) - 1u));
+}
+
+// Quad indices of corner row r (buffer.rs:288-372): corner order, then +x,
+// +y, +z; winding by dists[(x, y, z)] < 0.0.  Vertex ids are rowoff-based
+// minus `vbase`; quads are written from index 6 * q (capacity icap).
+__device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                              const float* __restrict__ dists,
+                                              const uint32_t* __restrict__ cellbits,
+                                              const uint32_t* __restrict__ wordoff,
+                                              const uint32_t* __restrict__ rowoff, uint32_t vbase,
+                                              uint64_t q, uint32_t* __restrict__ idx, uint64_t icap,
+                                              uint32_t r) {
+    const uint32_t x = r / d.res, y = r % d.res;
+    for (uint32_t w = 0; w < d.Wc; ++w) {
+        const EdgeWords e = edge_words(sgn, d, x, y, w);
+        uint32_t any = e.ex | e.ey | e.ez;
+        while (any) {
+            const uint32_t b = __ffs(any) - 1;
+            any &= any - 1;
+            const uint32_t z = w * 32 + b;
+            const bool neg = dists[((size_t)x * d.n + y) * d.n + z] < 0.0f;
+            const uint32_t bit = 1u << b;
+            uint32_t t[6];
+            if (e.ex & bit) {
+                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z - 1) - vbase;
+                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
+                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
+                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+                if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+                else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+                if (6 * q + 6 <= icap)
+                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                ++q;
+            }
+            if (e.ey & bit) {
+                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z - 1) - vbase;
+                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
+                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
+                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+                if (neg) { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+                else     { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+                if (6 * q + 6 <= icap)
+                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                ++q;
+            }
+            if (e.ez & bit) {
+                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y - 1, z) - vbase;
+                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
+                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
+                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+                if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+                else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+                if (6 * q + 6 <= icap)
+                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                ++q;
+            }
+        }
+    }
+}
+
+}  // namespace cg

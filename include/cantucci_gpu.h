@@ -184,6 +184,55 @@ cg_status cg_mesher_dists(cg_mesher* mesher, const float** dists, uint32_t* reso
  * of res^3 uint32, on the mesher's stream (synchronised before return). */
 cg_status cg_mesher_points(cg_mesher* mesher, uint32_t* points);
 
+/* ---- batched meshing ---------------------------------------------------- */
+
+/* One octree leaf to mesh: generate_for_box(&span, shape, resolution). */
+typedef struct cg_span_job {
+    cg_span span;
+    uint32_t resolution;
+    uint32_t reserved;
+} cg_span_job;
+
+/* Where one span's mesh landed in the batch outputs.  Its indices refer to
+ * its own vertices (0-based), exactly as that span's MeshBuffer would. */
+typedef struct cg_job_mesh {
+    uint64_t vertex_offset;
+    uint64_t index_offset;
+    uint32_t vertices;
+    uint32_t indices;
+} cg_job_mesh;
+
+typedef struct cg_batch cg_batch;
+
+/* Plans a batch of spans: the GPU form of ShapeMesh::update's thread pool,
+ * which runs one MeshBuffer::generate_for_box job per empty octree leaf
+ * (src/mesh/mod.rs:129-161).  Validates every job like generate_for_box
+ * (CG_EINVAL naming the job), uploads the span table and allocates the
+ * workspace, with room for `vertex_cap` vertices in total.  jobs: HOST. */
+cg_status cg_batch_create(int device, const cg_span_job* jobs, uint32_t n_jobs,
+                          uint64_t vertex_cap, cg_batch** out);
+void cg_batch_destroy(cg_batch* batch);
+
+/* Meshes every span of the batch: one persistent step-1 kernel pulling work
+ * from an atomic queue, then steps 2-3 over all spans.  Asynchronous on
+ * `stream`, no allocation, no host synchronisation (capturable).  DEVICE
+ * outputs: vertices / indices (written up to their capacities), results
+ * (n_jobs entries), totals (3 x uint32: vertices, quads, status bit 0 = a
+ * lerp factor left [0,1] in some span). */
+cg_status cg_batch_mesh(cg_batch* batch, const cg_shape* shape, cg_vertex* vertices,
+                        uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                        cg_job_mesh* results, uint32_t* totals, void* stream);
+
+/* Same, replayed from a CUDA graph: the first call (and any call whose
+ * arguments or batch options differ from the last) captures cg_batch_mesh
+ * into a graph; later calls launch that graph on `stream`. */
+cg_status cg_batch_mesh_graph(cg_batch* batch, const cg_shape* shape, cg_vertex* vertices,
+                              uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                              cg_job_mesh* results, uint32_t* totals, void* stream);
+
+/* Device pointer of job `job`'s corner distances after a cg_batch_mesh. */
+cg_status cg_batch_dists(cg_batch* batch, uint32_t job, const float** dists);
+
 /* ---- sphere tracing ----------------------------------------------------- */
 
 /* March loop of ShapeMesh::get_focii (src/mesh/mod.rs:229-241): for each ray
