@@ -82,6 +82,9 @@ SIGNATURES = [
     ("cg_batch_mesh_graph", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_dists", _i32, [_vp, _u32, C.POINTER(_vp)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
+    ("cg_de_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
+    ("cg_de_backward", _i32, [_shp, _vp, _vp, _u64, _vp, _vp, _vp]),
+    ("cg_fd_grad", _i32, [_shp, _vp, _u64, _f32, _vp, _vp]),
     ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),
     ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),
     ("cg_span_grid_work", _i32, [_shp, _spp, _u32, C.POINTER(_u64), C.POINTER(_u64)]),

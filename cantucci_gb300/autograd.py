@@ -1,0 +1,107 @@
+"""The distance estimator as a torch.autograd.Function.
+
+forward:  cg_min_distance_from (the polar-form estimator, f32).
+backward: cg_de_backward -- the hand-written adjoint kernel, which recomputes
+          the iterates from checkpoints instead of saving them -- giving
+          dL/dpoints and dL/d(power, euler angles).
+
+    power = torch.tensor(8.0, requires_grad=True)
+    rot = torch.zeros(3, requires_grad=True)
+    d = mandelbulb_de(points, power, rot, max_iters=15, bailout=2.5)
+    d.sum().backward()
+"""
+import ctypes as C
+
+from . import _ffi
+from ._ffi import check, load
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _shape(power: float, rot, max_iters: int, bailout: float) -> _ffi.CgShape:
+    s = _ffi.CgShape()
+    s.kind = _ffi.CG_SHAPE_MANDELBULB_POLAR
+    s.power = int(round(power))
+    s.power_f = float(power)
+    s.max_iters = int(max_iters)
+    s.bailout = float(bailout)
+    for k in range(3):
+        s.rot[k] = float(rot[k])
+    return s
+
+
+def _make_function():
+    torch = _torch()
+
+    class MandelbulbDE(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, points, power, rot, max_iters, bailout):
+            pts = points.detach().contiguous().float()
+            shape = _shape(float(power), [float(r) for r in rot.detach().cpu()], max_iters,
+                           bailout)
+            out = torch.empty(pts.shape[0], dtype=torch.float32, device=pts.device)
+            stream = torch.cuda.current_stream(pts.device)
+            check(load().cg_min_distance_from(C.byref(shape), C.c_void_p(pts.data_ptr()),
+                                              pts.shape[0], C.c_void_p(out.data_ptr()),
+                                              _ffi.CG_NUMERICS_EXACT,
+                                              C.c_void_p(stream.cuda_stream)))
+            ctx.save_for_backward(pts)  # the points only; no iterates
+            ctx.shape = shape
+            return out
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            (pts,) = ctx.saved_tensors
+            g = grad_out.detach().contiguous().float()
+            gp = torch.empty_like(pts) if ctx.needs_input_grad[0] else None
+            params = torch.empty(4, dtype=torch.float32, device=pts.device)
+            stream = torch.cuda.current_stream(pts.device)
+            check(load().cg_de_backward(C.byref(ctx.shape), C.c_void_p(pts.data_ptr()),
+                                        C.c_void_p(g.data_ptr()), pts.shape[0],
+                                        C.c_void_p(gp.data_ptr()) if gp is not None else None,
+                                        C.c_void_p(params.data_ptr()),
+                                        C.c_void_p(stream.cuda_stream)))
+            gpow = params[0] if ctx.needs_input_grad[1] else None
+            grot = params[1:4] if ctx.needs_input_grad[2] else None
+            return gp, gpow, grot, None, None
+
+    return MandelbulbDE
+
+
+_FN = None
+
+
+def mandelbulb_de(points, power, rot, max_iters: int = 15, bailout: float = 2.5):
+    """DE of (n, 3) CUDA points for a polar Mandelbulb with tensor parameters
+    `power` (scalar) and `rot` (3 Euler angles), differentiable in all three."""
+    global _FN
+    if _FN is None:
+        _FN = _make_function()
+    return _FN.apply(points, power, rot, max_iters, bailout)
+
+
+def de_grad(points, power: float, rot=(0.0, 0.0, 0.0), max_iters: int = 15,
+            bailout: float = 2.5):
+    """(n, 8) CUDA tensor: DE, dDE/dp (3), dDE/dpower, dDE/d(euler) (3)."""
+    torch = _torch()
+    pts = points.contiguous().float()
+    out = torch.empty((pts.shape[0], 8), dtype=torch.float32, device=pts.device)
+    shape = _shape(power, rot, max_iters, bailout)
+    check(load().cg_de_grad(C.byref(shape), C.c_void_p(pts.data_ptr()), pts.shape[0],
+                            C.c_void_p(out.data_ptr()),
+                            C.c_void_p(torch.cuda.current_stream(pts.device).cuda_stream)))
+    return out
+
+
+def fd_grad(points, shape, h: float):
+    """(n, 3) central-difference gradient with six estimator calls per point."""
+    torch = _torch()
+    pts = points.contiguous().float()
+    out = torch.empty((pts.shape[0], 3), dtype=torch.float32, device=pts.device)
+    check(load().cg_fd_grad(C.byref(shape._cshape()), C.c_void_p(pts.data_ptr()), pts.shape[0],
+                            float(h), C.c_void_p(out.data_ptr()),
+                            C.c_void_p(torch.cuda.current_stream(pts.device).cuda_stream)))
+    return out

@@ -1,0 +1,170 @@
+// adjoint.cu -- point kernels of the estimator's gradient (the adjoint in
+// adjoint.cuh), its batch vector-Jacobian product (the autograd backward),
+// and the six-evaluation central-difference gradient it replaces.
+#include <cmath>
+
+#include "adjoint.cuh"
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace cg {
+
+__global__ void __launch_bounds__(128) k_de_grad(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
+                                                 uint64_t n, float* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float o[8];
+        polar_de_grad(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) out[8 * i + k] = o[k];
+    }
+}
+
+// Vector-Jacobian product of a batch: g[i] * dDE/dp into grad_points (n x 3)
+// and the sum over points of g[i] * dDE/d(power, euler) into params (4
+// floats, accumulated with atomics; zero it first).
+__global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
+                                                const float* __restrict__ g, uint64_t n,
+                                                float* __restrict__ gp, float* __restrict__ params) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float o[8];
+        polar_de_grad(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
+        const float gi = g[i];
+        if (gp) {
+            gp[3 * i] = gi * o[1];
+            gp[3 * i + 1] = gi * o[2];
+            gp[3 * i + 2] = gi * o[3];
+        }
+        if (gi != 0.0f) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float v = gi * o[4 + k];
+                if (v == v) acc[k] += v;  // skip NaN (degenerate points)
+            }
+        }
+    }
+    if (params) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+            if ((threadIdx.x & 31) == 0 && v != 0.0f) atomicAdd(&params[k], v);
+        }
+    }
+}
+
+// Central-difference gradient with six estimator evaluations per point
+// (the normal of src/mesh/buffer.rs:256-266 with step h, divided by 2h).
+template <int M>
+__global__ void __launch_bounds__(128) k_fd_grad(ShapeDev s, const float* __restrict__ pts,
+                                                 uint64_t n, float h, float* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+        float g[3];
+#pragma unroll 1
+        for (int a = 0; a < 3; ++a) {
+            const float hx = a == 0 ? h : 0.0f, hy = a == 1 ? h : 0.0f, hz = a == 2 ? h : 0.0f;
+            const float dp = eval<M>(s, x + hx, y + hy, z + hz);
+            const float dm = eval<M>(s, x - hx, y - hy, z - hz);
+            g[a] = (dp - dm) / (2.0f * h);
+        }
+        out[3 * i] = g[0];
+        out[3 * i + 1] = g[1];
+        out[3 * i + 2] = g[2];
+    }
+}
+
+Dm3 rotation_derivatives(const cg_shape& c) {
+    Dm3 gs;
+    const double a = c.rot[0], b = c.rot[1], g = c.rot[2];
+    const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cc = cos(g), sc = sin(g);
+    const double d0[9] = {0, cc * sb * ca + sc * sa, -cc * sb * sa + sc * ca,
+                          0, sc * sb * ca - cc * sa, -sc * sb * sa - cc * ca,
+                          0, cb * ca,                -cb * sa};
+    const double d1[9] = {-cc * sb, cc * cb * sa, cc * cb * ca,
+                          -sc * sb, sc * cb * sa, sc * cb * ca,
+                          -cb,      -sb * sa,     -sb * ca};
+    const double d2[9] = {-sc * cb, -sc * sb * sa - cc * ca, -sc * sb * ca + cc * sa,
+                          cc * cb,  cc * sb * sa - sc * ca,  cc * sb * ca + sc * sa,
+                          0,        0,                       0};
+    for (int i = 0; i < 9; ++i) {
+        gs.m[i] = (float)d0[i];
+        gs.m[9 + i] = (float)d1[i];
+        gs.m[18 + i] = (float)d2[i];
+    }
+    return gs;
+}
+
+static cg_status check_grad_shape(const cg_shape* shape) {
+    if (!shape || shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
+        set_error("the adjoint is defined on the real-power polar Mandelbulb (kind 2)");
+        return CG_EINVAL;
+    }
+    if (shape->max_iters < 1 || shape->max_iters > ADJ_CK * ADJ_MAX_CK) {
+        set_error("adjoint supports 1 <= max_iters <= %d", ADJ_CK * ADJ_MAX_CK);
+        return CG_EINVAL;
+    }
+    return CG_OK;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" {
+
+cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, float* out,
+                     void* stream) {
+    CG_TRY(check_grad_shape(shape));
+    if (n && (!points || !out)) {
+        set_error("NULL buffer");
+        return CG_EINVAL;
+    }
+    if (!n) return CG_OK;
+    k_de_grad<<<grid_for(n, 128, 16), 128, 0, (cudaStream_t)stream>>>(
+        make_shape_dev(*shape), rotation_derivatives(*shape), points, n, out);
+    CG_CHECK_LAUNCH("k_de_grad");
+    return CG_OK;
+}
+
+cg_status cg_de_backward(const cg_shape* shape, const float* points, const float* grad_out,
+                         uint64_t n, float* grad_points, float* grad_params, void* stream) {
+    CG_TRY(check_grad_shape(shape));
+    if (n && (!points || !grad_out)) {
+        set_error("NULL buffer");
+        return CG_EINVAL;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (grad_params) CG_CUDA(cudaMemsetAsync(grad_params, 0, 4 * sizeof(float), st));
+    if (!n) return CG_OK;
+    k_de_vjp<<<grid_for(n, 128, 16), 128, 0, st>>>(make_shape_dev(*shape),
+                                                    rotation_derivatives(*shape), points,
+                                                    grad_out, n, grad_points, grad_params);
+    CG_CHECK_LAUNCH("k_de_vjp");
+    return CG_OK;
+}
+
+cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, float h, float* out,
+                     void* stream) {
+    if (!shape || (n && (!points || !out)) || !(h > 0.0f)) {
+        set_error("bad arguments to cg_fd_grad");
+        return CG_EINVAL;
+    }
+    if (!n) return CG_OK;
+    const ShapeDev s = make_shape_dev(*shape);
+    const unsigned G = grid_for(n, 128, 16);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    case MODE_P8: k_fd_grad<MODE_P8><<<G, 128, 0, st>>>(s, points, n, h, out); break;
+    case MODE_INT: k_fd_grad<MODE_INT><<<G, 128, 0, st>>>(s, points, n, h, out); break;
+    case MODE_POLAR: k_fd_grad<MODE_POLAR><<<G, 128, 0, st>>>(s, points, n, h, out); break;
+    default: k_fd_grad<MODE_SPHERE><<<G, 128, 0, st>>>(s, points, n, h, out); break;
+    }
+    CG_CHECK_LAUNCH("k_fd_grad");
+    return CG_OK;
+}
+
+}  // extern "C"

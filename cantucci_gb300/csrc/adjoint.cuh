@@ -1,0 +1,180 @@
+// adjoint.cuh -- reverse-mode gradient of the real-power polar estimator
+// (src/shape/mandelbulb.frag:1-39, rotated), shared by the point kernels
+// (adjoint.cu) and the depth-map backward (trace.cu).
+//
+// For the polar loop one thread returns, per point,
+//   DE, dDE/dp (3), dDE/dpower, dDE/d(euler angles) (3).
+// It is the adjoint of the forward loop, not a finite difference: the
+// forward pass keeps only a checkpoint of (z, dr) every ADJ_CK steps (in
+// registers / L1, never in HBM); the backward pass walks the segments from
+// last to first, recomputes each segment's iterates from its checkpoint and
+// back-propagates through them.  Work is about two forward passes plus one
+// backward pass, whatever max_iters is.
+//
+// Per step k (z_k -> z_{k+1} = r^P u(P theta, P phi) + q, dr_{k+1} =
+// r^(P-1) P dr_k + 1, r = |z_k|, theta = acos(z_z / r), phi = atan2(y, x)):
+//   q_bar     += z_bar
+//   g_zr       = z_bar . u,   g_th = zr (z_bar . du/dtheta'),  g_ph = zr (z_bar . du/dphi')
+//   r_bar     += g_zr P zr / r + dr_bar P dr (P - 1) r^(P-1) / r
+//   P_bar     += g_zr zr ln r + g_th theta + g_ph phi + dr_bar dr r^(P-1) (1 + P ln r)
+//   dr_bar     = dr_bar P r^(P-1)
+//   z_bar      = r_bar z / r + P g_th grad(theta) + P g_ph grad(phi)
+// The final DE = 0.5 r ln r / dr seeds r_bar = 0.5 (ln r + 1) / dr and
+// dr_bar = -DE / dr on the z whose |z| is the returned r (the escaping
+// iterate, or the stale one of the last step when the loop runs out).
+#pragma once
+
+#include <cmath>
+
+#include "de.cuh"
+
+namespace cg {
+
+constexpr int ADJ_CK = 4;        // checkpoint interval (steps)
+constexpr int ADJ_MAX_CK = 16;   // checkpoints: max_iters <= 64
+
+// dR/d(angle k) for k = a, b, c, row-major, 3 x 9 floats.
+struct Dm3 {
+    float m[27];
+};
+Dm3 rotation_derivatives(const cg_shape& c);
+
+struct StepState {
+    float x, y, z, dr;
+};
+
+// One forward step of the polar loop from (z, dr); returns false on escape
+// (r > bailout).  r is always returned.
+__device__ __forceinline__ bool polar_step(const ShapeDev& s, float qx, float qy, float qz,
+                                           StepState& st, float& r) {
+    r = magnitude<Exact>(st.x, st.y, st.z);
+    if (r > s.bailout) return false;
+    const float P = s.power_f;
+    float theta = acosf(__fdiv_rn(st.z, r));
+    float phi = atan2f(st.y, st.x);
+    st.dr = __fadd_rn(__fmul_rn(__fmul_rn(powf(r, __fsub_rn(P, 1.0f)), P), st.dr), 1.0f);
+    const float zr = powf(r, P);
+    theta = __fmul_rn(theta, P);
+    phi = __fmul_rn(phi, P);
+    float sn, cs, sp, cp;
+    sincosf(theta, &sn, &cs);
+    sincosf(phi, &sp, &cp);
+    st.x = __fadd_rn(__fmul_rn(zr, __fmul_rn(sn, cp)), qx);
+    st.y = __fadd_rn(__fmul_rn(zr, __fmul_rn(sp, sn)), qy);
+    st.z = __fadd_rn(__fmul_rn(zr, cs), qz);
+    return true;
+}
+
+__device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __restrict__ dm,
+                                              float px, float py, float pz, float* out) {
+    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+    const float qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    const float P = s.power_f;
+    const uint32_t N = s.max_iters;
+
+    // Forward with checkpoints.
+    StepState ck[ADJ_MAX_CK];
+    StepState st = {qx, qy, qz, 1.0f};
+    float r = 0.0f;
+    uint32_t K = 0;
+    bool escaped = false;
+    for (uint32_t i = 0; i < N; ++i) {
+        if (i % ADJ_CK == 0) ck[i / ADJ_CK] = st;
+        float ri;
+        const StepState before = st;
+        if (!polar_step(s, qx, qy, qz, st, ri)) {
+            r = ri;
+            escaped = true;
+            st = before;
+            break;
+        }
+        r = ri;
+        ++K;
+    }
+    // st = z_K (escaped) or z_N; r = |z_K| (escaped) or |z_{N-1}| (stale).
+    const float dr_fin = st.dr;
+    const float ln_r = logf(r);
+    const float de = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(ln_r, r)), dr_fin);
+    float r_seed = 0.5f * (ln_r + 1.0f) / dr_fin;
+    float drb = -de / dr_fin;
+    float zbx = 0.0f, zby = 0.0f, zbz = 0.0f;
+    if (escaped && r > 0.0f) {
+        zbx = r_seed * st.x / r;
+        zby = r_seed * st.y / r;
+        zbz = r_seed * st.z / r;
+        r_seed = 0.0f;
+    }
+    float qbx = 0.0f, qby = 0.0f, qbz = 0.0f, Pb = 0.0f;
+
+    // Backward, segment by segment.
+    StepState seg[ADJ_CK];
+    const int nseg = (int)((K + ADJ_CK - 1) / ADJ_CK);
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+        const uint32_t k0 = (uint32_t)sgi * ADJ_CK;
+        const uint32_t k1 = min(k0 + ADJ_CK, K);
+        StepState t = ck[sgi];
+        for (uint32_t k = k0; k < k1; ++k) {
+            seg[k - k0] = t;
+            float rr;
+            polar_step(s, qx, qy, qz, t, rr);
+        }
+        for (int kk = (int)(k1 - k0) - 1; kk >= 0; --kk) {
+            const uint32_t k = k0 + (uint32_t)kk;
+            const StepState z = seg[kk];
+            // q gets the "+ q" of this step.
+            qbx += zbx;
+            qby += zby;
+            qbz += zbz;
+            const float rk = sqrtf((z.x * z.x + z.y * z.y) + z.z * z.z);
+            const float rho2 = z.x * z.x + z.y * z.y;
+            const float rho = sqrtf(rho2);
+            const float theta = acosf(z.z / rk), phi = atan2f(z.y, z.x);
+            const float lnr = logf(rk);
+            const float t1 = powf(rk, P - 1.0f);  // r^(P-1)
+            const float zr = t1 * rk;               // r^P
+            float sn, cs, sp, cp;
+            sincosf(theta * P, &sn, &cs);
+            sincosf(phi * P, &sp, &cp);
+            const float g_zr = zbx * (sn * cp) + zby * (sn * sp) + zbz * cs;
+            const float g_th = zr * (zbx * (cs * cp) + zby * (cs * sp) - zbz * sn);
+            const float g_ph = zr * sn * (zby * cp - zbx * sp);
+            float rb = g_zr * P * t1 + drb * P * z.dr * (P - 1.0f) * t1 / rk;
+            if (!escaped && k + 1 == N) rb += r_seed;  // stale r belongs to this step
+            Pb += g_zr * zr * lnr + g_th * theta + g_ph * phi +
+                  drb * z.dr * t1 * (1.0f + P * lnr);
+            drb = drb * P * t1;
+            const float thb = P * g_th, phb = P * g_ph;
+            float gx = rb * z.x / rk, gy = rb * z.y / rk, gz = rb * z.z / rk;
+            if (rho > 1e-30f) {
+                const float inv_r2rho = 1.0f / (rk * rk * rho);
+                gx += thb * z.z * z.x * inv_r2rho - phb * z.y / rho2;
+                gy += thb * z.z * z.y * inv_r2rho + phb * z.x / rho2;
+                gz += -thb * rho / (rk * rk);
+            }
+            zbx = gx;
+            zby = gy;
+            zbz = gz;
+        }
+    }
+    // z_0 = q.
+    qbx += zbx;
+    qby += zby;
+    qbz += zbz;
+    out[0] = x86_nan(de);
+    // dDE/dp = R q_bar (q = R^T p).
+    out[1] = s.m[0] * qbx + s.m[1] * qby + s.m[2] * qbz;
+    out[2] = s.m[3] * qbx + s.m[4] * qby + s.m[5] * qbz;
+    out[3] = s.m[6] * qbx + s.m[7] * qby + s.m[8] * qbz;
+    out[4] = Pb;
+    for (int a = 0; a < 3; ++a) {
+        const float* d = dm + 9 * a;
+        // dq/d(angle) = (dR/d(angle))^T p
+        const float dqx = d[0] * px + d[3] * py + d[6] * pz;
+        const float dqy = d[1] * px + d[4] * py + d[7] * pz;
+        const float dqz = d[2] * px + d[5] * py + d[8] * pz;
+        out[5 + a] = qbx * dqx + qby * dqy + qbz * dqz;
+    }
+}
+
+}  // namespace cg

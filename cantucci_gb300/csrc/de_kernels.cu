@@ -222,9 +222,12 @@ __global__ void __launch_bounds__(256) k_de_grid_p8x2(ShapeDev s, GridDev g,
         const bool liveA = inYZ && xA < n, liveB = inYZ && xB < n;
         const float py = grid_coord(g, 1, y), pz = grid_coord(g, 2, z);
         float dA = 0.0f, dB = 0.0f;
+        // Both lanes always iterate a real corner (an inactive lane repeats
+        // the other's), so no code path sees a lane that is known to be idle.
+        const float pxA = grid_coord(g, 0, liveA ? xA : xB);
+        const float pxB = grid_coord(g, 0, liveB ? xB : xA);
         if (liveA || liveB)
-            mandelbulb_p8_x2(s.max_iters, s.bailout, liveA, liveB, grid_coord(g, 0, xA), py, pz,
-                             grid_coord(g, 0, xB), py, pz, dA, dB);
+            mandelbulb_p8_x2(s.max_iters, s.bailout, true, true, pxA, py, pz, pxB, py, pz, dA, dB);
         uint32_t bitA = 0, bitB = 0;
         if (liveA) {
             out[((size_t)xA * n + y) * n + z] = dA;

@@ -242,6 +242,57 @@ cg_status cg_march(const cg_shape* shape, const float* origins, const float* dir
                    uint32_t max_steps, float epsilon, float* hits, uint8_t* hit,
                    void* stream);
 
+/* A pinhole camera: eye looking at target, `up` hint, vertical field of view
+ * fov_y (radians), width x height pixels (row-major, row 0 at the top). */
+typedef struct cg_camera {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float fov_y;
+    uint32_t width;
+    uint32_t height;
+} cg_camera;
+
+/* Depth map by sphere tracing every pixel's ray: the march of
+ * ShapeMesh::get_focii (src/mesh/mod.rs:229-241) per pixel, hit when
+ * DE < eps_scale * t * (pixel angle), at most max_steps steps.
+ * depth: device, width*height floats, ray distance t or -1 for a miss. */
+cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_t max_steps,
+                         float eps_scale, float* depth, void* stream);
+
+/* Implicit-surface backward of cg_trace_depth for the polar shape: at a hit
+ * x = eye + t d, DE(x; theta) = 0 gives dt/dtheta = -(dDE/dtheta) /
+ * (grad_x DE . d).  Sums grad_depth[i] * dt_i/d(power, a, b, c) over hit
+ * pixels into grad_params (device, 4 floats).  No reference counterpart. */
+cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, const float* depth,
+                            const float* grad_depth, float* grad_params, void* stream);
+
+/* ---- gradients ---------------------------------------------------------- */
+
+/* Forward + reverse-mode adjoint of the real-power polar estimator
+ * (kind CG_SHAPE_MANDELBULB_POLAR, src/shape/mandelbulb.frag:1-39, rotated).
+ * No reference counterpart: it replaces the six extra estimator calls of the
+ * central-difference normal (src/mesh/buffer.rs:256-266) and gives the
+ * parameter gradients for fitting.  Iterates are recomputed from
+ * checkpoints, never stored.  max_iters <= 64.
+ * out: device, n x 8 floats: DE, dDE/dx, dDE/dy, dDE/dz, dDE/dpower,
+ * dDE/da, dDE/db, dDE/dc (Euler angles). */
+cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, float* out,
+                     void* stream);
+
+/* Backward of DE over a batch (the autograd.Function backward): given the
+ * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to
+ * grad_points (device n x 3, may be NULL) and the sums over i of
+ * g[i] * dDE/d(power, a, b, c) to grad_params (device, 4 floats, may be NULL). */
+cg_status cg_de_backward(const cg_shape* shape, const float* points, const float* grad_out,
+                         uint64_t n, float* grad_points, float* grad_params, void* stream);
+
+/* Central-difference gradient with six estimator calls per point and step h
+ * (the normal of src/mesh/buffer.rs:256-266, scaled by 1/2h), any shape.
+ * out: device, n x 3 floats. */
+cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, float h, float* out,
+                     void* stream);
+
 /* ---- measurement -------------------------------------------------------- */
 
 /* Process-wide tuning knobs.  "de_grid_kernel": 0 auto, 1 one corner per

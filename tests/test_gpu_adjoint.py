@@ -1,0 +1,126 @@
+"""Adjoint kernel against the FP64 forward-mode oracle and FP64 central
+differences, and the autograd.Function against torch's gradcheck-style
+finite differences of the forward.
+
+Tolerances: the estimator iterates a chaotic map, so f32 gradients carry the
+same amplified rounding as f32 distances.  On points near the surface (the
+band |DE| < 1e-3 the normals are used on) we require the f32 adjoint's
+normal to be within 0.1 degree of the FP64 one for >= 99% of points, and its
+power derivative within 1e-3 relative for >= 99%.
+"""
+import numpy as np
+import pytest
+
+from cantucci_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def angle_deg(a, b):
+    a = a / np.linalg.norm(a, axis=1, keepdims=True)
+    b = b / np.linalg.norm(b, axis=1, keepdims=True)
+    return np.degrees(np.arccos(np.clip(np.sum(a * b, axis=1), -1, 1)))
+
+
+def band_points(cg, n, power=8.0, rot=(0.0, 0.0, 0.0), seed=0):
+    """Points near the surface: uniform in the box, marched 8 steps along
+    random directions, then kept where |DE| < 1e-3."""
+    import torch
+    shape = cg.MandelbulbPolar(power, 15, 2.5, rot)
+    rng = np.random.default_rng(seed)
+    p = torch.as_tensor(rng.uniform(-1.2, 1.2, size=(8 * n, 3)).astype(np.float32)).cuda()
+    d = torch.as_tensor(rng.normal(size=(8 * n, 3)).astype(np.float32)).cuda()
+    d = d / d.norm(dim=1, keepdim=True)
+    for _ in range(8):
+        p = p + d * shape.batch_min_distance_from(p)[:, None]
+    de = shape.batch_min_distance_from(p)
+    keep = torch.isfinite(de) & (de.abs() < 1e-3)
+    return p[keep][:n].contiguous()
+
+
+def test_adjoint_matches_fp64_forward_mode(cg, orc):
+    import torch
+    from cantucci_gb300.autograd import de_grad
+    rot = (0.2, 0.1, 0.0)
+    pts = band_points(cg, 4000, 8.3, rot)
+    assert pts.shape[0] >= 1000
+    g = de_grad(pts, 8.3, rot).cpu().numpy().astype(np.float64)
+    ref = orc.de_grad_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), pts.cpu().numpy())
+    fin = np.all(np.isfinite(ref), axis=1) & np.all(np.isfinite(g), axis=1)
+    assert fin.mean() > 0.99
+    ang = angle_deg(g[fin, 1:4], ref[fin, 1:4])
+    assert np.mean(ang < 0.1) >= 0.99, np.quantile(ang, [0.5, 0.99])
+    rel = np.abs(g[fin, 4] - ref[fin, 4]) / np.maximum(np.abs(ref[fin, 4]), 1e-6)
+    assert np.mean(rel < 1e-3) >= 0.99, np.quantile(rel, [0.5, 0.99])
+    rot_err = np.abs(g[fin, 5:8] - ref[fin, 5:8]) / np.maximum(
+        np.linalg.norm(ref[fin, 5:8], axis=1, keepdims=True), 1e-6)
+    assert np.mean(np.all(rot_err < 1e-3, axis=1)) >= 0.99
+    # the DE itself is the forward estimator's value
+    d = cg.MandelbulbPolar(8.3, 15, 2.5, rot).batch_min_distance_from(pts).cpu().numpy()
+    np.testing.assert_array_equal(d.view(np.uint32), g[:, 0].astype(np.float32).view(np.uint32))
+
+
+def test_adjoint_matches_fp64_central_differences(cg, orc):
+    """Against FP64 central differences with h = 1e-4 (the benchmark's check),
+    where the DE is smooth at that scale."""
+    from cantucci_gb300.autograd import de_grad
+    pts = band_points(cg, 2000, 8.0, seed=1)
+    p64 = pts.cpu().numpy().astype(np.float64)
+    g = de_grad(pts, 8.0).cpu().numpy().astype(np.float64)
+    s = orc.mandelbulb_polar(8.0, 15, 2.5)
+    h = 1e-4
+    fd = np.zeros((len(p64), 3))
+    for a in range(3):
+        e = np.zeros(3)
+        e[a] = h
+        plus = np.array([orc.lib().orc_de_f64(s, *(p + e)) for p in p64])
+        minus = np.array([orc.lib().orc_de_f64(s, *(p - e)) for p in p64])
+        fd[:, a] = (plus - minus) / (2 * h)
+    ref = orc.de_grad_f64(s, pts.cpu().numpy())[:, 1:4]
+    smooth = angle_deg(fd, ref) < 0.1  # where h = 1e-4 resolves the gradient
+    assert smooth.mean() > 0.5
+    ang = angle_deg(g[smooth, 1:4], fd[smooth])
+    assert np.mean(ang < 0.1) >= 0.99
+
+
+def test_autograd_function(cg):
+    import torch
+    from cantucci_gb300.autograd import de_grad, mandelbulb_de
+    pts = band_points(cg, 512, 8.3, (0.2, 0.1, 0.0), seed=2).requires_grad_(True)
+    power = torch.tensor(8.3, requires_grad=True)
+    rot = torch.tensor([0.2, 0.1, 0.0], requires_grad=True)
+    w = torch.linspace(-1, 1, pts.shape[0], device=pts.device)
+    loss = (mandelbulb_de(pts, power, rot) * w).sum()
+    loss.backward()
+    full = de_grad(pts.detach(), 8.3, (0.2, 0.1, 0.0))
+    np.testing.assert_allclose(pts.grad.cpu().numpy(), (full[:, 1:4] * w[:, None]).cpu().numpy(),
+                               rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(float(power.grad), float((full[:, 4] * w).sum()), rtol=1e-3,
+                               atol=1e-4)
+    np.testing.assert_allclose(rot.grad.numpy(), (full[:, 5:8] * w[:, None]).sum(0).cpu().numpy(),
+                               rtol=1e-3, atol=1e-4)
+
+
+def test_fd_grad_matches_adjoint_on_smooth_points(cg):
+    """GPU six-evaluation central differences agree with the adjoint where
+    the field is smooth at the step."""
+    from cantucci_gb300.autograd import de_grad, fd_grad
+    pts = band_points(cg, 4000, 8.0, seed=3)
+    shape = cg.MandelbulbPolar(8.0, 15, 2.5)
+    a = de_grad(pts, 8.0).cpu().numpy()[:, 1:4]
+    f1 = fd_grad(pts, shape, 1e-3).cpu().numpy()
+    f2 = fd_grad(pts, shape, 5e-4).cpu().numpy()
+    smooth = angle_deg(f1, f2) < 0.05
+    assert np.median(angle_deg(a[smooth], f2[smooth])) < 0.5
+
+
+def test_adjoint_rejects_other_shapes(cg):
+    import torch
+    from cantucci_gb300.autograd import de_grad, _shape
+    import ctypes as C
+    from cantucci_gb300 import _ffi
+    s = cg.Mandelbulb(8, 15, 2.5)._cshape()
+    pts = torch.zeros((4, 3), device="cuda")
+    out = torch.empty((4, 8), device="cuda")
+    assert _ffi.load().cg_de_grad(C.byref(s), C.c_void_p(pts.data_ptr()), 4,
+                                  C.c_void_p(out.data_ptr()), None) == _ffi.CG_EINVAL
