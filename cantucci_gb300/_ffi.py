@@ -42,6 +42,11 @@ class CgTimings(C.Structure):
                 ("vertices", C.c_uint32), ("faces", C.c_uint32)]
 
 
+class CgCamera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_y", C.c_float), ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
 class CgSpanJob(C.Structure):
     _fields_ = [("span", CgSpan), ("resolution", C.c_uint32), ("reserved", C.c_uint32)]
 
@@ -82,6 +87,8 @@ SIGNATURES = [
     ("cg_batch_mesh_graph", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_dists", _i32, [_vp, _u32, C.POINTER(_vp)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
+    ("cg_trace_depth", _i32, [_shp, C.c_void_p, _u32, _f32, _vp, _vp]),
+    ("cg_trace_backward", _i32, [_shp, C.c_void_p, _vp, _vp, _vp, _vp]),
     ("cg_de_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
     ("cg_de_backward", _i32, [_shp, _vp, _vp, _u64, _vp, _vp, _vp]),
     ("cg_fd_grad", _i32, [_shp, _vp, _u64, _f32, _vp, _vp]),

@@ -1,0 +1,105 @@
+"""Sphere-traced depth maps and their implicit-surface gradient.
+
+The depth map is checked against an FP64 march of the same rays (the FP64
+oracle estimator); the backward against central differences of re-rendered
+depths on pixels whose depth is smooth in the parameter.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rays(cam):
+    """The pixel rays of cg_trace_depth's camera, in float64."""
+    W, H = cam.width, cam.height
+    eye = np.array(cam.eye[:], np.float64)
+    f = -eye / np.linalg.norm(eye)
+    up = np.array(cam.up[:], np.float64)
+    r = np.cross(f, up)
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    th = np.tan(0.5 * cam.fov_y)
+    j, i = np.meshgrid(np.arange(W), np.arange(H))
+    uu = ((j + 0.5) / W * 2 - 1) * th * (W / H)
+    vv = (1 - (i + 0.5) / H * 2) * th
+    d = f[None, None] + uu[..., None] * r + vv[..., None] * u
+    return eye, d / np.linalg.norm(d, axis=-1, keepdims=True)
+
+
+def march_f64(orc, shape, cam, max_steps=256, eps_scale=1e-4):
+    eye, d = rays(cam)
+    d = d.reshape(-1, 3)
+    pix = 2 * np.tan(0.5 * cam.fov_y) / cam.height
+    t = np.zeros(len(d))
+    out = np.full(len(d), -1.0)
+    live = np.ones(len(d), bool)
+    for _ in range(max_steps):
+        idx = np.nonzero(live)[0]
+        if len(idx) == 0:
+            break
+        p = eye[None] + t[idx, None] * d[idx]
+        de = orc.de_f64(shape, p.astype(np.float32))
+        hit = de < eps_scale * np.maximum(t[idx], 1e-3) * pix
+        out[idx[hit]] = t[idx[hit]]
+        live[idx[hit]] = False
+        t[idx[~hit]] += de[~hit]
+        gone = (t[idx] > 10) | ~np.isfinite(de)
+        live[idx[gone & ~hit]] = False
+    return out.reshape(cam.height, cam.width)
+
+
+def test_depth_map_matches_fp64_march(cg, orc):
+    from cantucci_gb300 import fit
+    cam = fit.camera(64, 64)
+    depth = fit.render(8.3, (0.2, 0.1, 0.0), cam).cpu().numpy()
+    ref = march_f64(orc, orc.mandelbulb_polar(8.3, 15, 2.5, (0.2, 0.1, 0.0)), cam)
+    both = (depth > 0) & (ref > 0)
+    assert np.mean((depth > 0) == (ref > 0)) > 0.97
+    assert both.sum() > 500
+    err = np.abs(depth[both] - ref[both])
+    assert np.median(err) < 1e-4 and np.mean(err < 1e-3) > 0.95
+
+
+def test_trace_backward_matches_central_differences(cg):
+    import torch
+    from cantucci_gb300 import fit
+    cam = fit.camera(128, 128)
+    rot = (0.2, 0.1, 0.0)
+    h = 1e-3
+    d0 = fit.render(8.3, rot, cam).cpu().numpy()
+    dp = fit.render(8.3 + h, rot, cam).cpu().numpy()
+    dm = fit.render(8.3 - h, rot, cam).cpu().numpy()
+    fd = (dp - dm) / (2 * h)
+    # pixels whose depth is smooth in the power at this step
+    dp2 = fit.render(8.3 + h / 2, rot, cam).cpu().numpy()
+    dm2 = fit.render(8.3 - h / 2, rot, cam).cpu().numpy()
+    fd2 = (dp2 - dm2) / h
+    ok = (d0 > 0) & (dp > 0) & (dm > 0) & (np.abs(fd - fd2) < 0.05 * np.abs(fd) + 1e-3)
+    assert ok.sum() > 1000
+    # implicit gradient, one pixel at a time through the batched backward
+    power = torch.tensor(8.3, requires_grad=True)
+    r = torch.tensor(rot, requires_grad=True)
+    depth = fit.depth_render(power, r, cam)
+    w = torch.zeros_like(depth)
+    sel = np.argwhere(ok)[:200]
+    got = []
+    for (i, j) in sel:
+        w.zero_()
+        w[i, j] = 1.0
+        power.grad = None
+        g = torch.autograd.grad(depth, power, grad_outputs=w, retain_graph=True)[0]
+        got.append(float(g))
+    got = np.array(got)
+    want = fd[sel[:, 0], sel[:, 1]]
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-3)
+    assert np.median(rel) < 0.05, np.quantile(rel, [0.5, 0.9])
+
+
+def test_fit_reduces_loss(cg):
+    from cantucci_gb300 import fit
+    cam = fit.camera(96, 96)
+    target = fit.render(8.3, (0.2, 0.1, 0.0), cam)
+    p, rot, losses = fit.fit(target, cam, steps=40, lr=1e-2)
+    assert losses[-1] < losses[0]
+    assert abs(p - 8.3) < abs(8.0 - 8.3)
