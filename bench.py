@@ -60,7 +60,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -161,6 +161,158 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- GPU extras
+def _time_cuda(fn, reps=3, warm=1, stream=None):
+    """Mean CUDA-event milliseconds of fn() over `reps` runs after `warm`."""
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    s = stream or torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        fn()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def extra_batched(dev):
+    """4096 seeded octree spans (res 8..64): one batch replayed from a CUDA
+    graph vs one cg_generate_for_box_device call per span."""
+    import numpy as np
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    from cantucci_gb300.batch import BatchMesher
+    spans, res, power, iters = W.batched_spans(4096, seed=0)
+    shape = cg.Mandelbulb(power, iters, 2.5)
+    corners = int(np.sum((res.astype(np.int64) + 1) ** 3))
+    b = BatchMesher(spans, res, vertex_cap=1 << 24, index_cap=6 << 24, device=dev)
+    ms_graph = _time_cuda(lambda: b.run(shape, graph=True), reps=5, warm=2)
+    ms_direct = _time_cuda(lambda: b.run(shape, graph=False), reps=3, warm=1)
+    _, tot = b.run(shape, graph=True).host()
+    m = cg.Mesher(dev)
+    v = torch.empty((64 ** 3, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(18 * 64 ** 3, dtype=torch.int32, device=dev)
+    t0 = time.perf_counter()
+    for sp, r in zip(spans, res):
+        m.generate_device(cg.Span(sp[:3], sp[3:]), shape, int(r), v, i, strict=False)
+    seq_s = time.perf_counter() - t0
+    m.close()
+    b.close()
+    return {"workload": "4096 spans, centres on the 0.8-1.15 shell, edge 2^-k k in 3..7, res in "
+                        "{8,16,32,64}, power %d, max_iters %d, seed 0" % (power, iters),
+            "corners": corners, "vertices": int(tot[0]), "quads": int(tot[1]),
+            "graph_ms": ms_graph, "direct_ms": ms_direct,
+            "spans_per_s": 4096 / (ms_graph * 1e-3), "corners_per_s": corners / (ms_graph * 1e-3),
+            "per_span_launches_s": seq_s, "per_span_spans_per_s": 4096 / seq_s,
+            "speedup_vs_per_span": seq_s / (ms_graph * 1e-3)}
+
+
+def band_points(shape, n, seed=1, oversample=6):
+    """n points drawn uniformly in [-1.2,1.2]^3, moved by 8 sphere-trace steps
+    along random unit directions, kept where |DE| < 1e-3."""
+    import numpy as np
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    keep = []
+    have = 0
+    while have < n:
+        m = oversample * n
+        p = torch.rand((m, 3), generator=g, device="cuda") * 2.4 - 1.2
+        d = torch.randn((m, 3), generator=g, device="cuda")
+        d = d / d.norm(dim=1, keepdim=True)
+        for _ in range(8):
+            p = p + d * shape.batch_min_distance_from(p)[:, None]
+        de = shape.batch_min_distance_from(p)
+        k = p[torch.isfinite(de) & (de.abs() < 1e-3)]
+        keep.append(k)
+        have += k.shape[0]
+    return torch.cat(keep)[:n].contiguous()
+
+
+def extra_normals(dev, n=16 << 20):
+    """Adjoint normals vs six-evaluation central differences on 16M band
+    points (polar form, power 8, max_iters 15), with angular errors against
+    the FP64 forward-mode oracle on a 2000-point subsample."""
+    import numpy as np
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300.autograd import de_grad, fd_grad
+    shape = cg.MandelbulbPolar(8.0, 15, 2.5)
+    pts = band_points(shape, n)
+    ms_fwd = _time_cuda(lambda: shape.batch_min_distance_from(pts), reps=2)
+    ms_adj = _time_cuda(lambda: de_grad(pts, 8.0), reps=2)
+    ms_fd = _time_cuda(lambda: fd_grad(pts, shape, 1e-4), reps=2)
+    out = {"workload": "%d points in |DE| < 1e-3 (uniform in [-1.2,1.2]^3, 8 sphere-trace steps "
+                       "along random directions), polar Mandelbulb power 8, max_iters 15" % n,
+           "forward_pts_per_s": n / (ms_fwd * 1e-3),
+           "fwd_adjoint_pts_per_s": n / (ms_adj * 1e-3),
+           "fd6_pts_per_s": n / (ms_fd * 1e-3),
+           "adjoint_vs_fd6_speedup": ms_fd / ms_adj}
+    try:
+        import oracle
+        sub = pts[:2000]
+        ref = oracle.de_grad_f64(oracle.mandelbulb_polar(8.0, 15, 2.5), sub.cpu().numpy())
+        a = de_grad(sub, 8.0).cpu().numpy().astype(np.float64)
+        f = fd_grad(sub, shape, 1e-4).cpu().numpy().astype(np.float64)
+
+        def ang(x, y):
+            x = x / np.linalg.norm(x, axis=1, keepdims=True)
+            y = y / np.linalg.norm(y, axis=1, keepdims=True)
+            return np.degrees(np.arccos(np.clip(np.sum(x * y, axis=1), -1, 1)))
+        ok = np.all(np.isfinite(ref[:, 1:4]), axis=1)
+        ea, ef = ang(a[ok, 1:4], ref[ok, 1:4]), ang(f[ok], ref[ok, 1:4])
+        out["angle_deg_vs_fp64"] = {
+            "adjoint": {"median": float(np.median(ea)), "p99": float(np.quantile(ea, 0.99)),
+                        "frac_le_0.1": float(np.mean(ea <= 0.1))},
+            "fd6_h1e-4": {"median": float(np.median(ef)), "p99": float(np.quantile(ef, 0.99)),
+                          "frac_le_0.1": float(np.mean(ef <= 0.1))}}
+    except Exception as e:  # the oracle is only a checker here
+        out["angle_deg_vs_fp64"] = "unavailable: %s" % e
+    return out
+
+
+def extra_depth_fit(dev, steps=300):
+    """1024x1024 depth map of power 8.3 rotated (0.2, 0.1, 0); fit power and
+    rotation from (8.0, 0) with Adam (lr 1e-2) on per-pixel L1 depth loss."""
+    import torch
+    from cantucci_gb300 import fit
+    cam = fit.camera(1024, 1024, 2.5, 60.0)
+    target = fit.render(8.3, (0.2, 0.1, 0.0), cam)
+    ms_fwd = _time_cuda(lambda: fit.render(8.3, (0.2, 0.1, 0.0), cam, out=target), reps=3)
+    power = torch.tensor(8.0, requires_grad=True)
+    rot = torch.zeros(3, requires_grad=True)
+    depth = fit.depth_render(power, rot, cam)
+    loss = fit.l1_loss(depth, target)
+    ms_bwd = _time_cuda(lambda: torch.autograd.grad(loss, [power, rot], retain_graph=True),
+                        reps=3)
+    t0 = time.perf_counter()
+    p, r, losses = fit.fit(target, cam, steps=steps, lr=1e-2)
+    fit_s = time.perf_counter() - t0
+    return {"workload": "1024x1024 depth map, camera at 2.5, fov 60 deg, <= 256 steps, eps 1e-4 "
+                        "pixel footprint, polar Mandelbulb power 8.3 rot (0.2, 0.1, 0), "
+                        "max_iters 15; Adam %d steps lr 1e-2 from power 8.0, rot 0" % steps,
+            "forward_pixels_per_s": 1024 * 1024 / (ms_fwd * 1e-3),
+            "backward_pixels_per_s": 1024 * 1024 / (ms_bwd * 1e-3),
+            "fit_seconds": fit_s, "recovered_power": p, "recovered_rotation": r,
+            "loss_first": losses[0], "loss_last": losses[-1]}
+
+
+def run_extras(args, dev):
+    out = {}
+    for name, fn in (("batched_spans", extra_batched), ("normals", extra_normals),
+                     ("depth_fit", extra_depth_fit)):
+        try:
+            out[name] = fn(dev)
+        except Exception as e:  # report, never hide the headline number
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+    return out
+
+
 # ---------------------------------------------------------------- GPU side
 def run_ours(args, rank, world, local_rank):
     import numpy as np
@@ -191,14 +343,16 @@ def run_ours(args, rank, world, local_rank):
     def step_device():
         return mesher.generate_device(span, shape, res, verts_d, idx_d, strict=False)
 
+    # Clocks are sampled from the warm-up through the end-to-end run, which
+    # brackets the timed region.
+    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dev)).split(",")[0])
+                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else dev)
+    clocks.start()
     for _ in range(args.warmup):
         step_device()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
-    clocks = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dev)).split(",")[0])
-                          if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else dev)
-    clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     stage = []
@@ -211,7 +365,6 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
-    clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     t_local = ms * 1e-3
     t_max = t_local
@@ -240,6 +393,7 @@ def run_ours(args, rank, world, local_rank):
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
+    clk = clocks.stop()
     e2e = {"value": world * n_pts * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": C.sizeof(_ffi.CgSpan) + C.sizeof(_ffi.CgShape),
            "d2h_bytes_per_step": nv * 28 + ni * 4 + 16,
@@ -297,6 +451,8 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roofline, "e2e": e2e, "clocks": clk,
         "gpu_launches": LAUNCHES_PER_MESH * args.steps,
     }
+    if rank == 0 and not args.no_extras:
+        line["extras"] = run_extras(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         r, threads, p, dt, text = cpu_mesh_sample(4)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
@@ -314,6 +470,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched, normals and depth-map measurements")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per k_de_grid launch from an ncu capture")
     args = ap.parse_args()

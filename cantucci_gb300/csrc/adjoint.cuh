@@ -65,6 +65,37 @@ __device__ __forceinline__ bool polar_step(const ShapeDev& s, float qx, float qy
     return true;
 }
 
+// A step's input and the values its forward computation produces.
+struct StepDeriv {
+    float x, y, z, dr;       // z_k, dr_k
+    float r, theta, phi;     // |z_k|, acos(z/r), atan2(y, x)
+    float t1, zr;            // r^(P-1), r^P
+    float sn, cs, sp, cp;    // sin/cos of P theta and P phi
+};
+
+// polar_step from `st`, recording the step into `d` (the step never escapes:
+// it is a recompute of a step the forward pass completed).
+__device__ __forceinline__ void polar_step_deriv(const ShapeDev& s, float qx, float qy, float qz,
+                                                 StepState& st, StepDeriv& d) {
+    d.x = st.x;
+    d.y = st.y;
+    d.z = st.z;
+    d.dr = st.dr;
+    const float P = s.power_f;
+    const float r = magnitude<Exact>(st.x, st.y, st.z);
+    d.r = r;
+    d.theta = acosf(__fdiv_rn(st.z, r));
+    d.phi = atan2f(st.y, st.x);
+    d.t1 = powf(r, __fsub_rn(P, 1.0f));
+    st.dr = __fadd_rn(__fmul_rn(__fmul_rn(d.t1, P), st.dr), 1.0f);
+    d.zr = powf(r, P);
+    sincosf(__fmul_rn(d.theta, P), &d.sn, &d.cs);
+    sincosf(__fmul_rn(d.phi, P), &d.sp, &d.cp);
+    st.x = __fadd_rn(__fmul_rn(d.zr, __fmul_rn(d.sn, d.cp)), qx);
+    st.y = __fadd_rn(__fmul_rn(d.zr, __fmul_rn(d.sp, d.sn)), qy);
+    st.z = __fadd_rn(__fmul_rn(d.zr, d.cs), qz);
+}
+
 __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __restrict__ dm,
                                               float px, float py, float pz, float* out) {
     const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
@@ -107,35 +138,31 @@ __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __
     }
     float qbx = 0.0f, qby = 0.0f, qbz = 0.0f, Pb = 0.0f;
 
-    // Backward, segment by segment.
-    StepState seg[ADJ_CK];
+    // Backward, segment by segment.  The recompute keeps each step's derived
+    // values (the ones the forward step computes anyway), so the backward
+    // step itself needs no transcendental function but one log.
+    StepDeriv seg[ADJ_CK];
     const int nseg = (int)((K + ADJ_CK - 1) / ADJ_CK);
     for (int sgi = nseg - 1; sgi >= 0; --sgi) {
         const uint32_t k0 = (uint32_t)sgi * ADJ_CK;
         const uint32_t k1 = min(k0 + ADJ_CK, K);
         StepState t = ck[sgi];
-        for (uint32_t k = k0; k < k1; ++k) {
-            seg[k - k0] = t;
-            float rr;
-            polar_step(s, qx, qy, qz, t, rr);
-        }
+        for (uint32_t k = k0; k < k1; ++k) polar_step_deriv(s, qx, qy, qz, t, seg[k - k0]);
         for (int kk = (int)(k1 - k0) - 1; kk >= 0; --kk) {
             const uint32_t k = k0 + (uint32_t)kk;
-            const StepState z = seg[kk];
+            const StepDeriv& z = seg[kk];
             // q gets the "+ q" of this step.
             qbx += zbx;
             qby += zby;
             qbz += zbz;
-            const float rk = sqrtf((z.x * z.x + z.y * z.y) + z.z * z.z);
+            const float rk = z.r;
             const float rho2 = z.x * z.x + z.y * z.y;
             const float rho = sqrtf(rho2);
-            const float theta = acosf(z.z / rk), phi = atan2f(z.y, z.x);
+            const float theta = z.theta, phi = z.phi;
             const float lnr = logf(rk);
-            const float t1 = powf(rk, P - 1.0f);  // r^(P-1)
-            const float zr = t1 * rk;               // r^P
-            float sn, cs, sp, cp;
-            sincosf(theta * P, &sn, &cs);
-            sincosf(phi * P, &sp, &cp);
+            const float t1 = z.t1;  // r^(P-1)
+            const float zr = z.zr;  // r^P
+            const float sn = z.sn, cs = z.cs, sp = z.sp, cp = z.cp;
             const float g_zr = zbx * (sn * cp) + zby * (sn * sp) + zbz * cs;
             const float g_th = zr * (zbx * (cs * cp) + zby * (cs * sp) - zbz * sn);
             const float g_ph = zr * sn * (zby * cp - zbx * sp);
