@@ -64,6 +64,14 @@ class ClockSampler:
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # nvidia-smi takes a moment to print its first sample; the timed
+        # region starts only once sampling runs.
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.02)
 
     def stop(self):
         if self.proc is None:
@@ -314,6 +322,14 @@ def run_extras(args, dev):
 
 
 # ---------------------------------------------------------------- GPU side
+def _measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -429,6 +445,17 @@ def run_ours(args, rank, world, local_rank):
     }
     if args.traffic is not None:
         roofline["traffic"] = args.traffic
+    # The same kernel against HBM: it writes one f32 distance per corner and
+    # the packed sign words (one bit per corner, rows padded to 32 bits).
+    grid_bytes = 4 * n_pts + 4 * (res + 1) ** 2 * ((res + 1 + 31) // 32)
+    hbm_peak = _measured_hbm_gbs()
+    roofline["hbm_view"] = {
+        "algorithmic_bytes_per_launch": grid_bytes,
+        "achieved_gbs": grid_bytes / (de_ms * 1e-3) / 1e9,
+        "peak_gbs": hbm_peak, "frac": (grid_bytes / (de_ms * 1e-3) / 1e9 / hbm_peak
+                                       if hbm_peak else None),
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)" if hbm_peak else None,
+    }
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -50,6 +50,8 @@ def _make_function():
                                               C.c_void_p(stream.cuda_stream)))
             ctx.save_for_backward(pts)  # the points only; no iterates
             ctx.shape = shape
+            ctx.param_devices = (power.device if torch.is_tensor(power) else None,
+                                 rot.device if torch.is_tensor(rot) else None)
             return out
 
         @staticmethod
@@ -64,8 +66,9 @@ def _make_function():
                                         C.c_void_p(gp.data_ptr()) if gp is not None else None,
                                         C.c_void_p(params.data_ptr()),
                                         C.c_void_p(stream.cuda_stream)))
-            gpow = params[0] if ctx.needs_input_grad[1] else None
-            grot = params[1:4] if ctx.needs_input_grad[2] else None
+            pdev, rdev = ctx.param_devices
+            gpow = params[0].to(pdev) if ctx.needs_input_grad[1] else None
+            grot = params[1:4].to(rdev) if ctx.needs_input_grad[2] else None
             return gp, gpow, grot, None, None
 
     return MandelbulbDE

@@ -67,11 +67,14 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t n = g.n;
     const uint32_t BX = (n + 1) >> 1, BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
-    const uint32_t bricks = BX * BY * BZ;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
-    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < bricks; b += nwarps) {
-        const uint32_t bz = b % BZ, t = b / BZ, by = t % BY, bx = t / BY;
+    // Brick (bx, by, bz) of this warp, advanced by the grid stride written in
+    // the same mixed radix, so the loop does no integer division.
+    const uint32_t b0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t bz = b0 % BZ, by = (b0 / BZ) % BY, bx = b0 / (BZ * BY);
+    const uint32_t sz = nwarps % BZ, sy = (nwarps / BZ) % BY, sx = nwarps / (BZ * BY);
+    for (; bx < BX;) {
         const uint32_t x = 2 * bx + dx, y = 4 * by + dy, z = 4 * bz + dz;
         const bool active = x < n && y < n && z < n;
         uint32_t bit = 0;
@@ -85,6 +88,19 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
             bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 2);
             if (dz == 0 && bit) atomicOr(&sgn[(x * n + y) * W + (z >> 5)], bit);
         }
+        bz += sz;
+        uint32_t carry = 0;
+        if (bz >= BZ) {
+            bz -= BZ;
+            carry = 1;
+        }
+        by += sy + carry;
+        carry = 0;
+        if (by >= BY) {
+            by -= BY;
+            carry = 1;
+        }
+        bx += sx + carry;
     }
 }
 

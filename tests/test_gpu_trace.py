@@ -1,8 +1,9 @@
 """Sphere-traced depth maps and their implicit-surface gradient.
 
 The depth map is checked against an FP64 march of the same rays (the FP64
-oracle estimator); the backward against central differences of re-rendered
-depths on pixels whose depth is smooth in the parameter.
+oracle estimator); the backward against the FP64 implicit-surface gradient at
+the same hit points and, loosely, central differences of re-rendered depths
+on pixels whose depth is smooth in the parameter.
 """
 import numpy as np
 import pytest
@@ -61,7 +62,15 @@ def test_depth_map_matches_fp64_march(cg, orc):
     assert np.median(err) < 1e-4 and np.mean(err < 1e-3) > 0.95
 
 
-def test_trace_backward_matches_central_differences(cg):
+def test_trace_backward_matches_fp64_implicit_gradient(cg, orc):
+    """Per pixel, the backward's d(depth)/d(power, euler) equals the FP64
+    implicit-surface formula -(dDE/dtheta) / (grad_x DE . d) at the same hit
+    point, and it tracks central differences of re-rendered depth maps.
+
+    The second check is loose on purpose: a rendered depth is the march's
+    last t, whose derivative also carries the sphere-tracing history (each
+    step's DE depends on the parameters), while the implicit gradient is that
+    of the level set through the hit point, the quantity a fit wants."""
     import torch
     from cantucci_gb300 import fit
     cam = fit.camera(128, 128)
@@ -71,13 +80,12 @@ def test_trace_backward_matches_central_differences(cg):
     dp = fit.render(8.3 + h, rot, cam).cpu().numpy()
     dm = fit.render(8.3 - h, rot, cam).cpu().numpy()
     fd = (dp - dm) / (2 * h)
-    # pixels whose depth is smooth in the power at this step
     dp2 = fit.render(8.3 + h / 2, rot, cam).cpu().numpy()
     dm2 = fit.render(8.3 - h / 2, rot, cam).cpu().numpy()
     fd2 = (dp2 - dm2) / h
+    # pixels whose rendered depth is smooth in the power at this step
     ok = (d0 > 0) & (dp > 0) & (dm > 0) & (np.abs(fd - fd2) < 0.05 * np.abs(fd) + 1e-3)
-    assert ok.sum() > 1000
-    # implicit gradient, one pixel at a time through the batched backward
+    assert ok.sum() > 300
     power = torch.tensor(8.3, requires_grad=True)
     r = torch.tensor(rot, requires_grad=True)
     depth = fit.depth_render(power, r, cam)
@@ -87,13 +95,27 @@ def test_trace_backward_matches_central_differences(cg):
     for (i, j) in sel:
         w.zero_()
         w[i, j] = 1.0
-        power.grad = None
-        g = torch.autograd.grad(depth, power, grad_outputs=w, retain_graph=True)[0]
-        got.append(float(g))
+        gp, gr = torch.autograd.grad(depth, (power, r), grad_outputs=w, retain_graph=True)
+        got.append([float(gp)] + gr.tolist())
     got = np.array(got)
-    want = fd[sel[:, 0], sel[:, 1]]
-    rel = np.abs(got - want) / np.maximum(np.abs(want), 1e-3)
-    assert np.median(rel) < 0.05, np.quantile(rel, [0.5, 0.9])
+    # FP64 implicit gradient at the same hit points
+    eye, dirs = rays(cam)
+    dsel = dirs[sel[:, 0], sel[:, 1]]
+    hit = eye[None] + d0[sel[:, 0], sel[:, 1], None] * dsel
+    g64 = orc.de_grad_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), hit)
+    want = -g64[:, 4:8] / np.sum(g64[:, 1:4] * dsel, axis=1, keepdims=True)
+    rel_p = np.abs(got[:, 0] - want[:, 0]) / np.maximum(np.abs(want[:, 0]), 1e-3)
+    assert np.median(rel_p) < 1e-2 and np.mean(rel_p < 0.1) >= 0.85, \
+        np.quantile(rel_p, [0.5, 0.85])
+    rel_r = np.max(np.abs(got[:, 1:] - want[:, 1:]), axis=1) / np.maximum(
+        np.linalg.norm(want[:, 1:], axis=1), 1e-3)
+    assert np.median(rel_r) < 1e-2 and np.mean(rel_r < 0.1) >= 0.85, \
+        np.quantile(rel_r, [0.5, 0.85])
+    # against the rendered depth's own change
+    fdr = fd[sel[:, 0], sel[:, 1]]
+    relfd = np.abs(got[:, 0] - fdr) / np.maximum(np.abs(fdr), 1e-3)
+    assert np.median(relfd) < 0.3, np.quantile(relfd, [0.5, 0.9])
+    assert np.mean(np.sign(got[:, 0]) == np.sign(fdr)) > 0.8
 
 
 def test_fit_reduces_loss(cg):
