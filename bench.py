@@ -37,8 +37,11 @@ WORKLOAD = ("single octree span, 512^3 cells / 513^3 = 135,005,697 corners, Mand
 FLOPS_PER_STEP = 76   # P=8 iteration: magnitude, dr, polynomial, + p (each op = 1 flop)
 FLOPS_PER_ESCAPE = 6  # the final magnitude of an escaping point
 FLOPS_PER_POINT = 4   # ln(r) * r, * 0.5, / dr
-LAUNCHES_PER_MESH = 13  # k_de_grid, k_sign_words, k_cells, 3x scan, k_vertex_list, k_place,
-#                         k_quad_count, 3x scan, k_quad_emit
+# DRAM bytes of one k_de_grid_brick launch on the 513^3-corner span, from ncu:
+# 78,348,032 read + 560,385,024 written (algorithmic: 557,918,280 written).
+DE_TRAFFIC_RES512 = 78_348_032 + 560_385_024
+LAUNCHES_PER_MESH = 12  # k_de_grid_brick (sign words fused), k_cells, 3x scan, k_vertex_list,
+#                         k_place, k_quad_count, 3x scan, k_quad_emit (ncu launch list: 12 per mesh)
 
 
 # ---------------------------------------------------------------- clocks
@@ -113,7 +116,7 @@ def leaf_spans(depth: int = 3):
     return level
 
 
-def cpu_mesh_sample(stride: int = 4, threads: int = None):
+def cpu_mesh_sample(stride: int = 1, threads: int = None):
     """The reference's CPU path on a bounded sample of the same workload: the
     512 depth-3 octree leaves of the span (res 64 each, the same cell size as
     res 512 over the whole span), every `stride`-th leaf, one leaf per worker
@@ -136,9 +139,10 @@ def cpu_mesh_sample(stride: int = 4, threads: int = None):
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         pts = sum(ex.map(one, leaves))
     dt = time.perf_counter() - t0
-    text = ("%d of the 512 depth-3 octree leaves of the span (every %dth), res 64 each (%d "
-            "corners), oracle C restatement of generate_for_box, one leaf per thread" %
-            (len(leaves), stride, pts))
+    which = ("all 512 depth-3 octree leaves of the span" if stride == 1 else
+             "%d of the 512 depth-3 octree leaves of the span (every %dth)" % (len(leaves), stride))
+    text = ("%s, res 64 each (%d corners), oracle C restatement of generate_for_box, one leaf "
+            "per thread" % (which, pts))
     return pts / dt, threads, pts, dt, text
 
 
@@ -146,7 +150,7 @@ def run_reference(args, rank, world):
     """--impl reference: the CPU mesher on all host cores, rank 0 only."""
     if rank != 0:
         return
-    stride = 4
+    stride = 1  # all 512 leaves: the whole span at the cell size of res 512
     for _ in range(args.warmup):
         cpu_mesh_sample(stride)
     rates, secs, pts, threads, text = [], 0.0, 0, 0, ""
@@ -445,6 +449,12 @@ def run_ours(args, rank, world, local_rank):
     }
     if args.traffic is not None:
         roofline["traffic"] = args.traffic
+        roofline["traffic_source"] = "--traffic (DRAM bytes per launch from an ncu capture)"
+    elif res == RES:
+        roofline["traffic"] = DE_TRAFFIC_RES512
+        roofline["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                      "k_de_grid_brick launch at res 512 (ncu --set full, "
+                                      "profiles/k_de_grid_brick_res512.md)")
     # The same kernel against HBM: it writes one f32 distance per corner and
     # the packed sign words (one bit per corner, rows padded to 32 bits).
     grid_bytes = 4 * n_pts + 4 * (res + 1) ** 2 * ((res + 1 + 31) // 32)
@@ -481,7 +491,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_extras:
         line["extras"] = run_extras(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r, threads, p, dt, text = cpu_mesh_sample(4)
+        r, threads, p, dt, text = cpu_mesh_sample(1)
         line["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": text, "seconds": dt}
     if rank == 0:
