@@ -203,9 +203,31 @@ def extra_batched(dev):
     shape = cg.Mandelbulb(power, iters, 2.5)
     corners = int(np.sum((res.astype(np.int64) + 1) ** 3))
     b = BatchMesher(spans, res, vertex_cap=1 << 24, index_cap=6 << 24, device=dev)
+    default_tuning = b.tuning
+    ms_default = _time_cuda(lambda: b.run(shape, graph=True), reps=5, warm=2)
+    t0 = time.perf_counter()
+    tuned = b.autotune(shape, reps=3)
+    tune_s = time.perf_counter() - t0
     ms_graph = _time_cuda(lambda: b.run(shape, graph=True), reps=5, warm=2)
     ms_direct = _time_cuda(lambda: b.run(shape, graph=False), reps=3, warm=1)
-    _, tot = b.run(shape, graph=True).host()
+    out = b.run(shape, graph=True)
+    _, tot = out.host()
+    # the CPU builder (oracle restatement of generate_for_box) on every span,
+    # one span per host thread, and index lists compared on a sample
+    import oracle
+    oshape = oracle.mandelbulb(power, iters, 2.5)
+    oracle.lib()
+    threads = os.cpu_count() or 1
+
+    def cpu_one(j):
+        r = oracle.generate_for_box(oshape, spans[j].astype(np.float32), int(res[j]), nthreads=1,
+                                    vcap=int(res[j]) ** 3, icap=18 * int(res[j]) ** 3)
+        return r
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        cpu = list(ex.map(cpu_one, range(len(res))))
+    cpu_s = time.perf_counter() - t0
+    same = sum(int(np.array_equal(out.mesh(j)[1], cpu[j]["indices"])) for j in range(0, len(res), 16))
     m = cg.Mesher(dev)
     v = torch.empty((64 ** 3, 7), dtype=torch.float32, device=dev)
     i = torch.empty(18 * 64 ** 3, dtype=torch.int32, device=dev)
@@ -218,7 +240,12 @@ def extra_batched(dev):
     return {"workload": "4096 spans, centres on the 0.8-1.15 shell, edge 2^-k k in 3..7, res in "
                         "{8,16,32,64}, power %d, max_iters %d, seed 0" % (power, iters),
             "corners": corners, "vertices": int(tot[0]), "quads": int(tot[1]),
-            "graph_ms": ms_graph, "direct_ms": ms_direct,
+            "graph_ms": ms_graph, "direct_ms": ms_direct, "graph_ms_default_tuning": ms_default,
+            "default_tuning": default_tuning, "tuning": tuned["tuning"],
+            "autotune_s": tune_s,
+            "cpu_builder_s": cpu_s, "cpu_builder_threads": threads,
+            "cpu_builder_spans_per_s": 4096 / cpu_s, "speedup_vs_cpu_builder": cpu_s / (ms_graph * 1e-3),
+            "index_lists_equal_cpu_builder": "%d of %d sampled spans" % (same, len(range(0, len(res), 16))),
             "spans_per_s": 4096 / (ms_graph * 1e-3), "corners_per_s": corners / (ms_graph * 1e-3),
             "per_span_launches_s": seq_s, "per_span_spans_per_s": 4096 / seq_s,
             "speedup_vs_per_span": seq_s / (ms_graph * 1e-3)}
@@ -258,18 +285,28 @@ def extra_normals(dev, n=16 << 20):
     pts = band_points(shape, n)
     ms_fwd = _time_cuda(lambda: shape.batch_min_distance_from(pts), reps=2)
     ms_adj = _time_cuda(lambda: de_grad(pts, 8.0), reps=2)
+    ms_tan = _time_cuda(lambda: de_grad(pts, 8.0, mode="tangent", with_power=False), reps=2)
+    ms_tan4 = _time_cuda(lambda: de_grad(pts, 8.0, mode="tangent"), reps=2)
     ms_fd = _time_cuda(lambda: fd_grad(pts, shape, 1e-4), reps=2)
     out = {"workload": "%d points in |DE| < 1e-3 (uniform in [-1.2,1.2]^3, 8 sphere-trace steps "
                        "along random directions), polar Mandelbulb power 8, max_iters 15" % n,
            "forward_pts_per_s": n / (ms_fwd * 1e-3),
            "fwd_adjoint_pts_per_s": n / (ms_adj * 1e-3),
+           "fwd_tangent_normals_pts_per_s": n / (ms_tan * 1e-3),
+           "fwd_tangent_all_pts_per_s": n / (ms_tan4 * 1e-3),
            "fd6_pts_per_s": n / (ms_fd * 1e-3),
-           "adjoint_vs_fd6_speedup": ms_fd / ms_adj}
+           "adjoint_vs_fd6_speedup": ms_fd / ms_adj,
+           "tangent_normals_vs_fd6_speedup": ms_fd / ms_tan,
+           "tangent_all_vs_fd6_speedup": ms_fd / ms_tan4,
+           "modes": "adjoint = reverse mode with checkpoint recompute (DE, grad, d/dpower, "
+                    "d/drotation); tangent_normals = forward mode along x, y, z (DE, grad, "
+                    "d/drotation); tangent_all = forward mode with the power direction too"}
     try:
         import oracle
         sub = pts[:2000]
         ref = oracle.de_grad_f64(oracle.mandelbulb_polar(8.0, 15, 2.5), sub.cpu().numpy())
         a = de_grad(sub, 8.0).cpu().numpy().astype(np.float64)
+        t = de_grad(sub, 8.0, mode="tangent", with_power=False).cpu().numpy().astype(np.float64)
         f = fd_grad(sub, shape, 1e-4).cpu().numpy().astype(np.float64)
 
         def ang(x, y):
@@ -277,12 +314,17 @@ def extra_normals(dev, n=16 << 20):
             y = y / np.linalg.norm(y, axis=1, keepdims=True)
             return np.degrees(np.arccos(np.clip(np.sum(x * y, axis=1), -1, 1)))
         ok = np.all(np.isfinite(ref[:, 1:4]), axis=1)
-        ea, ef = ang(a[ok, 1:4], ref[ok, 1:4]), ang(f[ok], ref[ok, 1:4])
+        def stats(e):
+            return {"median": float(np.median(e)), "p99": float(np.quantile(e, 0.99)),
+                    "frac_le_0.1": float(np.mean(e <= 0.1))}
         out["angle_deg_vs_fp64"] = {
-            "adjoint": {"median": float(np.median(ea)), "p99": float(np.quantile(ea, 0.99)),
-                        "frac_le_0.1": float(np.mean(ea <= 0.1))},
-            "fd6_h1e-4": {"median": float(np.median(ef)), "p99": float(np.quantile(ef, 0.99)),
-                          "frac_le_0.1": float(np.mean(ef <= 0.1))}}
+            "adjoint": stats(ang(a[ok, 1:4], ref[ok, 1:4])),
+            "tangent": stats(ang(t[ok, 1:4], ref[ok, 1:4])),
+            "fd6_h1e-4": stats(ang(f[ok], ref[ok, 1:4]))}
+        # no step size brings the f32 central difference to the adjoint's error
+        for h in (1e-2, 1e-3, 3e-4, 3e-5, 1e-5):
+            fh = fd_grad(sub, shape, h).cpu().numpy().astype(np.float64)
+            out["angle_deg_vs_fp64"]["fd6_h%g" % h] = stats(ang(fh[ok], ref[ok, 1:4]))
     except Exception as e:  # the oracle is only a checker here
         out["angle_deg_vs_fp64"] = "unavailable: %s" % e
     return out

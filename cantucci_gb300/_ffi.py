@@ -56,6 +56,14 @@ class CgJobMesh(C.Structure):
                 ("vertices", C.c_uint32), ("indices", C.c_uint32)]
 
 
+class CgBatchTuning(C.Structure):
+    _fields_ = [("de_block", C.c_uint32), ("de_chunk", C.c_uint32),
+                ("brick_min_res", C.c_uint32), ("place_block", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
 VERTEX_DTYPE = np.dtype([("position", "<f4", (3,)), ("normal", "<f4", (3,)),
                          ("distance_from_surface", "<f4")])
 
@@ -86,10 +94,15 @@ SIGNATURES = [
     ("cg_batch_mesh", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_mesh_graph", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_dists", _i32, [_vp, _u32, C.POINTER(_vp)]),
+    ("cg_batch_get_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
+    ("cg_batch_set_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
+    ("cg_batch_autotune", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp, _u32,
+                                 C.POINTER(CgBatchTuning), C.POINTER(_f32)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
     ("cg_trace_depth", _i32, [_shp, C.c_void_p, _u32, _f32, _vp, _vp]),
     ("cg_trace_backward", _i32, [_shp, C.c_void_p, _vp, _vp, _vp, _vp]),
     ("cg_de_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
+    ("cg_de_grad_tangent", _i32, [_shp, _vp, _u64, _u32, _vp, _vp]),
     ("cg_de_backward", _i32, [_shp, _vp, _vp, _u64, _vp, _vp, _vp]),
     ("cg_fd_grad", _i32, [_shp, _vp, _u64, _f32, _vp, _vp]),
     ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),

@@ -87,15 +87,27 @@ def mandelbulb_de(points, power, rot, max_iters: int = 15, bailout: float = 2.5)
 
 
 def de_grad(points, power: float, rot=(0.0, 0.0, 0.0), max_iters: int = 15,
-            bailout: float = 2.5):
-    """(n, 8) CUDA tensor: DE, dDE/dp (3), dDE/dpower, dDE/d(euler) (3)."""
+            bailout: float = 2.5, mode: str = "adjoint", with_power: bool = True):
+    """(n, 8) CUDA tensor: DE, dDE/dp (3), dDE/dpower, dDE/d(euler) (3).
+
+    mode "adjoint": reverse mode with checkpoint recompute (cg_de_grad).
+    mode "tangent": forward mode, one pass (cg_de_grad_tangent); with
+    with_power=False it skips the power direction (column 4 is 0), which is
+    all a normal needs."""
     torch = _torch()
     pts = points.contiguous().float()
     out = torch.empty((pts.shape[0], 8), dtype=torch.float32, device=pts.device)
     shape = _shape(power, rot, max_iters, bailout)
-    check(load().cg_de_grad(C.byref(shape), C.c_void_p(pts.data_ptr()), pts.shape[0],
-                            C.c_void_p(out.data_ptr()),
-                            C.c_void_p(torch.cuda.current_stream(pts.device).cuda_stream)))
+    stream = C.c_void_p(torch.cuda.current_stream(pts.device).cuda_stream)
+    if mode == "adjoint":
+        check(load().cg_de_grad(C.byref(shape), C.c_void_p(pts.data_ptr()), pts.shape[0],
+                                C.c_void_p(out.data_ptr()), stream))
+    elif mode == "tangent":
+        check(load().cg_de_grad_tangent(C.byref(shape), C.c_void_p(pts.data_ptr()),
+                                        pts.shape[0], int(bool(with_power)),
+                                        C.c_void_p(out.data_ptr()), stream))
+    else:
+        raise ValueError("mode is 'adjoint' or 'tangent'")
     return out
 
 

@@ -7,8 +7,14 @@ which runs one MeshBuffer::generate_for_box job per empty octree leaf
     vertices, indices = out.mesh(j)              # span j's MeshBuffer contents
 
 `run(graph=True)` replays the whole batch from a CUDA graph.
+`autotune(shape)` picks the batch's launch shapes by timing it
+(cg_batch_autotune), remembering the winner in a small JSON cache keyed by
+the GPU, the shape and the batch's resolution histogram.
 """
 import ctypes as C
+import hashlib
+import json
+import os
 
 import numpy as np
 
@@ -67,6 +73,7 @@ class BatchMesher:
         res = np.asarray(resolutions, np.uint32).reshape(-1)
         assert len(spans) == len(res) and len(res) > 0
         self.n_jobs = len(res)
+        self._resolutions = res.copy()
         jobs = (_ffi.CgSpanJob * self.n_jobs)()
         for j in range(self.n_jobs):
             for k in range(3):
@@ -97,6 +104,61 @@ class BatchMesher:
             self.close()
         except Exception:
             pass
+
+    @property
+    def tuning(self) -> dict:
+        t = _ffi.CgBatchTuning()
+        check(self._lib.cg_batch_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **knobs):
+        t = _ffi.CgBatchTuning(**{**self.tuning, **knobs})
+        check(self._lib.cg_batch_set_tuning(self.handle, C.byref(t)))
+
+    def tuning_key(self, shape) -> str:
+        """Cache key: GPU name and SM count, the shape, the resolutions."""
+        torch = _torch()
+        p = torch.cuda.get_device_properties(self.device)
+        c = shape._cshape()
+        h = hashlib.sha256(np.sort(self._resolutions).tobytes()).hexdigest()[:16]
+        return "%s/%d/kind%d-p%d-%.4f-it%d/n%d-%s" % (p.name, p.multi_processor_count, c.kind,
+                                                      c.power, c.power_f, c.max_iters,
+                                                      self.n_jobs, h)
+
+    def autotune(self, shape, reps=3, cache_path=None, stream=None) -> dict:
+        """Picks and applies launch shapes for `shape` on this batch.
+
+        With `cache_path` (default: $CANTUCCI_TUNING_CACHE when set) a
+        previous winner for the same key is applied without timing, and a
+        new winner is stored.  Returns {"tuning", "ms", "cached"}."""
+        torch = _torch()
+        cache_path = cache_path or os.environ.get("CANTUCCI_TUNING_CACHE")
+        key = self.tuning_key(shape)
+        cache = {}
+        if cache_path and os.path.exists(cache_path):
+            with open(cache_path) as f:
+                cache = json.load(f)
+            if key in cache:
+                self.set_tuning(**cache[key]["tuning"])
+                return {"tuning": self.tuning, "ms": cache[key]["ms"], "cached": True}
+        stream = stream or torch.cuda.current_stream(self.device)
+        best = _ffi.CgBatchTuning()
+        ms = C.c_float()
+        check(self._lib.cg_batch_autotune(
+            self.handle, C.byref(shape._cshape()), C.c_void_p(self._verts.data_ptr()),
+            self.vertex_cap, C.c_void_p(self._idx.data_ptr()), self.index_cap,
+            C.c_void_p(self._res.data_ptr()), C.c_void_p(self._tot.data_ptr()),
+            C.c_void_p(stream.cuda_stream), int(reps), C.byref(best), C.byref(ms)))
+        out = {"tuning": best.as_dict(), "ms": float(ms.value), "cached": False}
+        if cache_path:
+            cache[key] = {"tuning": out["tuning"], "ms": out["ms"]}
+            d = os.path.dirname(os.path.abspath(cache_path))
+            os.makedirs(d, exist_ok=True)
+            tmp = cache_path + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(cache, f, indent=1, sort_keys=True)
+            os.replace(tmp, cache_path)
+        return out
 
     def run(self, shape, graph=False, stream=None) -> BatchResult:
         torch = _torch()

@@ -1,6 +1,7 @@
 // adjoint.cu -- point kernels of the estimator's gradient (the adjoint in
-// adjoint.cuh), its batch vector-Jacobian product (the autograd backward),
-// and the six-evaluation central-difference gradient it replaces.
+// adjoint.cuh and its forward-mode twin), its batch vector-Jacobian product
+// (the autograd backward), and the six-evaluation central-difference
+// gradient they replace.
 #include <cmath>
 
 #include "adjoint.cuh"
@@ -15,6 +16,19 @@ __global__ void __launch_bounds__(128) k_de_grad(ShapeDev s, Dm3 dm, const float
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         float o[8];
         polar_de_grad(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) out[8 * i + k] = o[k];
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(128) k_de_grad_tangent(ShapeDev s, Dm3 dm,
+                                                         const float* __restrict__ pts, uint64_t n,
+                                                         float* __restrict__ out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float o[8];
+        polar_de_tangent<T>(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
 #pragma unroll
         for (int k = 0; k < 8; ++k) out[8 * i + k] = o[k];
     }
@@ -127,6 +141,29 @@ cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, flo
     k_de_grad<<<grid_for(n, 128, 16), 128, 0, (cudaStream_t)stream>>>(
         make_shape_dev(*shape), rotation_derivatives(*shape), points, n, out);
     CG_CHECK_LAUNCH("k_de_grad");
+    return CG_OK;
+}
+
+cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
+                             uint32_t with_power, float* out, void* stream) {
+    if (!shape || shape->kind != CG_SHAPE_MANDELBULB_POLAR || shape->max_iters < 1) {
+        set_error("the gradient is defined on the real-power polar Mandelbulb (kind 2)");
+        return CG_EINVAL;
+    }
+    if (n && (!points || !out)) {
+        set_error("NULL buffer");
+        return CG_EINVAL;
+    }
+    if (!n) return CG_OK;
+    const unsigned G = grid_for(n, 128, 16);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (with_power)
+        k_de_grad_tangent<4><<<G, 128, 0, st>>>(make_shape_dev(*shape),
+                                                rotation_derivatives(*shape), points, n, out);
+    else
+        k_de_grad_tangent<3><<<G, 128, 0, st>>>(make_shape_dev(*shape),
+                                                rotation_derivatives(*shape), points, n, out);
+    CG_CHECK_LAUNCH("k_de_grad_tangent");
     return CG_OK;
 }
 

@@ -204,4 +204,112 @@ __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __
     }
 }
 
+// Forward (tangent) mode of the same loop: one pass carries the derivative
+// of (z, dr) along T directions next to the iterate -- dq = e_x, e_y, e_z
+// and, with T = 4, d(power) -- so nothing is stored or recomputed.  The
+// loop state and DE are those of polar_de (same exact operations); the
+// tangent updates use contracted arithmetic.  Per step and direction:
+//   r'   = (z . z') / r
+//   th'  = (z_z (x x' + y y') / rho - rho z_z') / r^2,  ph' = (x y' - y x') / rho^2
+//   zr'  = P r^(P-1) r' (+ r^P ln r P')
+//   Z'   = zr' u + zr ((P th' + th P') du/dTh + (P ph' + ph P') du/dPh) + q'
+//   dr'' = P (P-1) r^(P-2) dr r' + P r^(P-1) dr' (+ r^(P-1) dr (1 + P ln r) P')
+// and at the end DE' = 0.5 (ln r + 1) r' / dr - DE dr' / dr (the quotient
+// rule on DE = 0.5 r ln r / dr).  Outputs as polar_de_grad; with T = 3 there
+// is no power direction and out[4] = 0 (the rotation derivatives need only
+// the three point directions).  Work: one forward pass plus T tangent
+// updates of ~30 operations per step, against polar_de_grad's two forward
+// passes plus one backward step.
+template <int T>
+__device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float* __restrict__ dm,
+                                                 float px, float py, float pz, float* out) {
+    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+    const float qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    const float P = s.power_f;
+    float zx = qx, zy = qy, zz = qz, dr = 1.0f, r = 0.0f;
+    // tangents: direction k has (tx, ty, tz, tdr); dq_k = e_k for k < 3
+    float tx[T], ty[T], tz[T], tdr[T], tr[T];
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+        tx[k] = k == 0 ? 1.0f : 0.0f;
+        ty[k] = k == 1 ? 1.0f : 0.0f;
+        tz[k] = k == 2 ? 1.0f : 0.0f;
+        tdr[k] = 0.0f;
+        tr[k] = 0.0f;
+    }
+    for (uint32_t i = 0; i < s.max_iters; ++i) {
+        r = magnitude<Exact>(zx, zy, zz);
+        const float inv_r = 1.0f / r;
+#pragma unroll
+        for (int k = 0; k < T; ++k) tr[k] = (zx * tx[k] + zy * ty[k] + zz * tz[k]) * inv_r;
+        if (r > s.bailout) break;
+        const float theta = acosf(__fdiv_rn(zz, r));
+        const float phi = atan2f(zy, zx);
+        const float t1 = powf(r, __fsub_rn(P, 1.0f));
+        const float dr_old = dr;
+        dr = __fadd_rn(__fmul_rn(__fmul_rn(t1, P), dr), 1.0f);
+        const float zr = powf(r, P);
+        float sn, cs, sp, cp;
+        sincosf(__fmul_rn(theta, P), &sn, &cs);
+        sincosf(__fmul_rn(phi, P), &sp, &cp);
+        // shared factors of the tangent step
+        const float rho2 = zx * zx + zy * zy;
+        const float rho = sqrtf(rho2);
+        const bool off_axis = rho > 1e-30f;
+        const float inv_rho = off_axis ? 1.0f / rho : 0.0f;
+        const float inv_rho2 = off_axis ? 1.0f / rho2 : 0.0f;
+        const float inv_r2 = inv_r * inv_r;
+        const float Pt1 = P * t1;
+        const float k_dr = Pt1 * (P - 1.0f) * inv_r * dr_old;  // d(dr')/dr
+        // u and its derivatives, scaled by zr
+        const float ux = sn * cp, uy = sp * sn, uz = cs;
+        const float ax = zr * cs * cp, ay = zr * sp * cs, az = -zr * sn;  // zr du/dTh
+        const float bx = -zr * sn * sp, by = zr * cp * sn;                // zr du/dPh
+        float lnr = 0.0f;
+        if (T == 4) lnr = logf(r);
+#pragma unroll
+        for (int k = 0; k < T; ++k) {
+            const float th_t = (zz * (zx * tx[k] + zy * ty[k]) * inv_rho - rho * tz[k]) * inv_r2;
+            const float ph_t = (zx * ty[k] - zy * tx[k]) * inv_rho2;
+            float zr_t = Pt1 * tr[k];
+            float Th_t = P * th_t, Ph_t = P * ph_t;
+            float dr_t = k_dr * tr[k] + Pt1 * tdr[k];
+            if (T == 4 && k == 3) {  // the power direction
+                zr_t += zr * lnr;
+                Th_t += theta;
+                Ph_t += phi;
+                dr_t += t1 * dr_old * (1.0f + P * lnr);
+            }
+            tx[k] = zr_t * ux + Th_t * ax + Ph_t * bx + (k == 0 ? 1.0f : 0.0f);
+            ty[k] = zr_t * uy + Th_t * ay + Ph_t * by + (k == 1 ? 1.0f : 0.0f);
+            tz[k] = zr_t * uz + Th_t * az + (k == 2 ? 1.0f : 0.0f);
+            tdr[k] = dr_t;
+        }
+        zx = __fadd_rn(__fmul_rn(zr, __fmul_rn(sn, cp)), qx);
+        zy = __fadd_rn(__fmul_rn(zr, __fmul_rn(sp, sn)), qy);
+        zz = __fadd_rn(__fmul_rn(zr, cs), qz);
+    }
+    // tr holds r' of the returned r: the escaping iterate's, or the stale
+    // one of the last step when the loop runs out (tdr is then dr_N's).
+    const float ln_r = logf(r);
+    const float de = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(ln_r, r)), dr);
+    const float c_r = 0.5f * (ln_r + 1.0f) / dr, c_dr = -de / dr;
+    float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int k = 0; k < T; ++k) g[k] = c_r * tr[k] + c_dr * tdr[k];
+    out[0] = x86_nan(de);
+    out[1] = s.m[0] * g[0] + s.m[1] * g[1] + s.m[2] * g[2];
+    out[2] = s.m[3] * g[0] + s.m[4] * g[1] + s.m[5] * g[2];
+    out[3] = s.m[6] * g[0] + s.m[7] * g[1] + s.m[8] * g[2];
+    out[4] = g[3];
+    for (int a = 0; a < 3; ++a) {
+        const float* d = dm + 9 * a;
+        const float dqx = d[0] * px + d[3] * py + d[6] * pz;
+        const float dqy = d[1] * px + d[4] * py + d[7] * pz;
+        const float dqz = d[2] * px + d[5] * py + d[8] * pz;
+        out[5 + a] = g[0] * dqx + g[1] * dqy + g[2] * dqz;
+    }
+}
+
 }  // namespace cg

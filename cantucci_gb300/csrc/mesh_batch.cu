@@ -15,6 +15,12 @@
 //            (and, for quads, its index range) in span order.
 // No launch depends on a host-side count, so a batch is captured into one
 // CUDA graph and replayed.
+//
+// Launch shapes are per batch (cg_batch_tuning: step-1 block size and queue
+// chunk, the resolution from which spans use bricks, the placement block
+// size).  cg_batch_autotune picks them by timing the batch itself:
+// coordinate descent over a small candidate list, one knob at a time.  No
+// knob changes any output bit.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -45,25 +51,29 @@ struct BatchTotals {
     uint32_t vertices, quads, status, queue;
 };
 
-// Tuning knobs (cg_set_option "batch_chunk", "batch_block", "batch_brick_min_res").
-static uint32_t g_batch_chunk = 64;
-static uint32_t g_batch_block = 256;
-static uint32_t g_batch_brick_min_res = 32;
+// Defaults of new batches (cg_set_option "batch_chunk", "batch_block",
+// "batch_brick_min_res", "batch_place_block").
+static cg_batch_tuning g_batch_default = {256, 64, 32, 128};
+
+static bool valid_block(int64_t v, int64_t hi) {
+    return v >= 64 && v <= hi && (v & (v - 1)) == 0;
+}
+
+static bool valid_tuning(const cg_batch_tuning& t) {
+    return valid_block(t.de_block, 512) && t.de_chunk >= 1 && t.de_chunk <= 4096 &&
+           t.brick_min_res >= 2 && t.brick_min_res <= (1u << 20) && valid_block(t.place_block, 256);
+}
 
 int set_batch_option(const char* name, int64_t v) {
-    if (!strcmp(name, "batch_chunk") && v >= 1 && v <= 4096) {
-        g_batch_chunk = (uint32_t)v;
-        return 1;
-    }
-    if (!strcmp(name, "batch_block") && (v == 64 || v == 128 || v == 256 || v == 512)) {
-        g_batch_block = (uint32_t)v;
-        return 1;
-    }
-    if (!strcmp(name, "batch_brick_min_res") && v >= 2 && v <= 2048) {
-        g_batch_brick_min_res = (uint32_t)v;
-        return 1;
-    }
-    return 0;
+    cg_batch_tuning t = g_batch_default;
+    if (!strcmp(name, "batch_chunk")) t.de_chunk = (uint32_t)v;
+    else if (!strcmp(name, "batch_block")) t.de_block = (uint32_t)v;
+    else if (!strcmp(name, "batch_brick_min_res")) t.brick_min_res = (uint32_t)v;
+    else if (!strcmp(name, "batch_place_block")) t.place_block = (uint32_t)v;
+    else return 0;
+    if (v < 1 || v > (1 << 20) || !valid_tuning(t)) return 0;
+    g_batch_default = t;
+    return 1;
 }
 
 // Index of the last entry of a non-decreasing table with key <= v.
@@ -161,7 +171,7 @@ __global__ void k_batch_vertex_list(const BatchJob* __restrict__ jobs, uint32_t 
 }
 
 template <int M>
-__global__ void __launch_bounds__(128) k_batch_place(ShapeDev s, const BatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(256) k_batch_place(ShapeDev s, const BatchJob* __restrict__ jobs,
                                                      const float* __restrict__ dists,
                                                      const uint32_t* __restrict__ cellidx,
                                                      const uint32_t* __restrict__ celljob,
@@ -244,7 +254,10 @@ struct cg_batch {
     uint32_t *cellidx = nullptr, *celljob = nullptr, *scratch = nullptr;
     BatchTotals* tot = nullptr;
     size_t sgn_words = 0;
-    std::vector<uint32_t> res;  // per job, host copy
+    std::vector<uint32_t> res;    // per job, host copy
+    std::vector<BatchJob> hjobs;  // host copy of the span table
+    cg_batch_tuning tune = {256, 64, 32, 128};
+    uint32_t planned_brick_min_res = 0;  // the threshold the device table holds
     // graph cache
     cudaGraphExec_t exec = nullptr;
     unsigned char graph_key[160] = {0};
@@ -267,6 +280,71 @@ struct DeviceScope {
 
 size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Step-1 work items of every job for a brick threshold: 2x4x4 bricks for
+// res >= brick_min_res, runs of 32 corners in GridTable order below it.
+cg_status plan_items(std::vector<BatchJob>& jobs, uint32_t brick_min_res, uint32_t* total) {
+    uint64_t items = 0;
+    for (BatchJob& J : jobs) {
+        const uint64_t n = J.d.n;
+        J.brick = J.d.res >= brick_min_res ? 1u : 0u;
+        J.items = J.brick ? (uint32_t)(((n + 1) >> 1) * ((n + 3) >> 2) * ((n + 3) >> 2))
+                          : (uint32_t)((n * n * n + 31) / 32);
+        J.item_begin = (uint32_t)items;
+        items += J.items;
+        if (items > 0x7FFFFFFFull) {
+            set_error("batch too large: %llu step-1 work items", (unsigned long long)items);
+            return CG_EINVAL;
+        }
+    }
+    *total = (uint32_t)items;
+    return CG_OK;
+}
+
+// Brings the device span table in line with the batch's brick threshold
+// (synchronous; never called while a capture is running).
+cg_status sync_plan(cg_batch* b) {
+    if (b->planned_brick_min_res == b->tune.brick_min_res) return CG_OK;
+    uint32_t total = 0;
+    CG_TRY(plan_items(b->hjobs, b->tune.brick_min_res, &total));
+    CG_CUDA(cudaMemcpy(b->jobs, b->hjobs.data(), sizeof(BatchJob) * b->njobs,
+                       cudaMemcpyHostToDevice));
+    b->total_items = total;
+    b->planned_brick_min_res = b->tune.brick_min_res;
+    return CG_OK;
+}
+
+// Resident blocks per SM of a kernel at a block size (cached per device).
+template <class K>
+unsigned resident_grid(K kernel, unsigned block) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)block, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    return (unsigned)(sm_count() * per_sm);
+}
+
+template <int M>
+cg_status launch_batch_de(cg_batch* b, const ShapeDev& s, cudaStream_t st) {
+    const unsigned B = b->tune.de_block;
+    const unsigned G = resident_grid(k_batch_de<M>, B);
+    k_batch_de<M><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, b->tune.de_chunk, b->tot,
+                                   b->dists, b->sgn);
+    CG_CHECK_LAUNCH("k_batch_de");
+    return CG_OK;
+}
+
+template <int M>
+cg_status launch_batch_place(cg_batch* b, const ShapeDev& s, cg_vertex* vertices,
+                             uint64_t vertex_cap, cudaStream_t st) {
+    const unsigned B = b->tune.place_block;
+    const unsigned G = resident_grid(k_batch_place<M>, B);
+    k_batch_place<M><<<G, B, 0, st>>>(s, b->jobs, b->dists, b->cellidx, b->celljob, b->tot,
+                                      vertices, vertex_cap);
+    CG_CHECK_LAUNCH("k_batch_place");
+    return CG_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -279,7 +357,7 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
     }
     *out = nullptr;
     std::vector<BatchJob> jobs(n_jobs);
-    uint64_t dist = 0, sgnw = 0, cw = 0, rows = 0, items = 0;
+    uint64_t dist = 0, sgnw = 0, cw = 0, rows = 0;
     for (uint32_t i = 0; i < n_jobs; ++i) {
         const cg_span_job& hj = host_jobs[i];
         const uint32_t res = hj.resolution;
@@ -308,28 +386,28 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
         J.sgn_off = sgnw;
         J.cw_off = cw;
         J.row_begin = (uint32_t)rows;
-        J.item_begin = (uint32_t)items;
-        J.brick = res >= g_batch_brick_min_res ? 1u : 0u;
-        J.items = J.brick ? (uint32_t)(((n + 1) >> 1) * ((n + 3) >> 2) * ((n + 3) >> 2))
-                          : (uint32_t)((n * n * n + 31) / 32);
         dist += n * n * n;
         sgnw += n * n * J.d.W;
         cw += (uint64_t)res * res * J.d.Wc;
         rows += (uint64_t)res * res;
-        items += J.items;
-        if (rows > (16u << 20) || items > 0x7FFFFFFFu || dist > 0xFFFFFFFFull * 4) {
+        if (rows > (16u << 20) || dist > 0xFFFFFFFFull * 4) {
             set_error("batch too large: %llu cell rows", (unsigned long long)rows);
             return CG_EINVAL;
         }
     }
+    const cg_batch_tuning tune = g_batch_default;
+    uint32_t items = 0;
+    CG_TRY(plan_items(jobs, tune.brick_min_res, &items));
     cg_batch* b = new (std::nothrow) cg_batch();
     if (!b) return CG_ENOMEM;
     b->device = device;
     b->njobs = n_jobs;
-    b->total_items = (uint32_t)items;
+    b->total_items = items;
     b->rows = (uint32_t)rows;
     b->vertex_cap = vertex_cap;
     b->sgn_words = sgnw;
+    b->tune = tune;
+    b->planned_brick_min_res = tune.brick_min_res;
     b->res.resize(n_jobs);
     for (uint32_t i = 0; i < n_jobs; ++i) b->res[i] = host_jobs[i].resolution;
     size_t off = 0;
@@ -368,6 +446,7 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
         delete b;
         return st;
     }
+    b->hjobs = std::move(jobs);
     *out = b;
     return CG_OK;
 }
@@ -380,12 +459,37 @@ void cg_batch_destroy(cg_batch* b) {
     delete b;
 }
 
+cg_status cg_batch_get_tuning(const cg_batch* b, cg_batch_tuning* t) {
+    if (!b || !t) {
+        set_error("bad arguments to cg_batch_get_tuning");
+        return CG_EINVAL;
+    }
+    *t = b->tune;
+    return CG_OK;
+}
+
+cg_status cg_batch_set_tuning(cg_batch* b, const cg_batch_tuning* t) {
+    if (!b || !t || !valid_tuning(*t)) {
+        set_error("bad batch tuning: de_block and place_block are powers of two in [64, 512] "
+                  "and [64, 256], de_chunk in [1, 4096], brick_min_res in [2, 2^20]");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceScope g(b->device);
+    b->tune = *t;
+    return sync_plan(b);
+}
+
 cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
                         uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
                         cg_job_mesh* results, uint32_t* totals, void* stream) {
     if (!b || !shape || !results || !totals || (vertex_cap && !vertices) ||
         (index_cap && !indices)) {
         set_error("bad arguments to cg_batch_mesh");
+        return CG_EINVAL;
+    }
+    if (b->planned_brick_min_res != b->tune.brick_min_res) {
+        set_error("batch span table out of date (cg_batch_set_tuning did not finish)");
         return CG_EINVAL;
     }
     if (vertex_cap > b->vertex_cap) vertex_cap = b->vertex_cap;
@@ -396,31 +500,13 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     }
     const ShapeDev s = make_shape_dev(*shape);
     cudaStream_t st = (cudaStream_t)stream;
-    const unsigned B = g_batch_block;
     CG_CUDA(cudaMemsetAsync(b->tot, 0, sizeof(BatchTotals), st));
     CG_CUDA(cudaMemsetAsync(b->sgn, 0, b->sgn_words * 4, st));
-    {
-        const unsigned G = (unsigned)sm_count() * (2048 / B);
-        const uint32_t chunk = g_batch_chunk;
-        switch (mode_of(s, CG_NUMERICS_EXACT)) {
-        case MODE_P8:
-            k_batch_de<MODE_P8><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk, b->tot,
-                                                 b->dists, b->sgn);
-            break;
-        case MODE_INT:
-            k_batch_de<MODE_INT><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
-                                                  b->tot, b->dists, b->sgn);
-            break;
-        case MODE_POLAR:
-            k_batch_de<MODE_POLAR><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
-                                                    b->tot, b->dists, b->sgn);
-            break;
-        default:
-            k_batch_de<MODE_SPHERE><<<G, B, 0, st>>>(s, b->jobs, b->njobs, b->total_items, chunk,
-                                                     b->tot, b->dists, b->sgn);
-            break;
-        }
-        CG_CHECK_LAUNCH("k_batch_de");
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    case MODE_P8: CG_TRY(launch_batch_de<MODE_P8>(b, s, st)); break;
+    case MODE_INT: CG_TRY(launch_batch_de<MODE_INT>(b, s, st)); break;
+    case MODE_POLAR: CG_TRY(launch_batch_de<MODE_POLAR>(b, s, st)); break;
+    default: CG_TRY(launch_batch_de<MODE_SPHERE>(b, s, st)); break;
     }
     const unsigned G = grid_for(b->rows, 256, 8);
     k_batch_cells<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->cellbits, b->wordoff,
@@ -430,28 +516,11 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     k_batch_vertex_list<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->cellbits, b->wordoff,
                                            b->rowoff, vertex_cap, b->cellidx, b->celljob);
     CG_CHECK_LAUNCH("k_batch_vertex_list");
-    {
-        const unsigned GP = (unsigned)sm_count() * 16;
-        switch (mode_of(s, CG_NUMERICS_EXACT)) {
-        case MODE_P8:
-            k_batch_place<MODE_P8><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
-                                                       b->celljob, b->tot, vertices, vertex_cap);
-            break;
-        case MODE_INT:
-            k_batch_place<MODE_INT><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
-                                                        b->celljob, b->tot, vertices, vertex_cap);
-            break;
-        case MODE_POLAR:
-            k_batch_place<MODE_POLAR><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
-                                                          b->celljob, b->tot, vertices, vertex_cap);
-            break;
-        default:
-            k_batch_place<MODE_SPHERE><<<GP, 128, 0, st>>>(s, b->jobs, b->dists, b->cellidx,
-                                                           b->celljob, b->tot, vertices,
-                                                           vertex_cap);
-            break;
-        }
-        CG_CHECK_LAUNCH("k_batch_place");
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    case MODE_P8: CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st)); break;
+    case MODE_INT: CG_TRY(launch_batch_place<MODE_INT>(b, s, vertices, vertex_cap, st)); break;
+    case MODE_POLAR: CG_TRY(launch_batch_place<MODE_POLAR>(b, s, vertices, vertex_cap, st)); break;
+    default: CG_TRY(launch_batch_place<MODE_SPHERE>(b, s, vertices, vertex_cap, st)); break;
     }
     k_batch_quad_count<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->quadcnt);
     CG_CHECK_LAUNCH("k_batch_quad_count");
@@ -475,8 +544,8 @@ cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* ver
     }
     std::lock_guard<std::mutex> lk(b->mu);
     DeviceScope g(b->device);
-    // The graph bakes in every argument and the tuning knobs: recapture when
-    // any of them changes.
+    // The graph bakes in every argument and the launch shapes: recapture
+    // when any of them changes.
     unsigned char key[160];
     memset(key, 0, sizeof key);
     size_t o = 0;
@@ -491,9 +560,7 @@ cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* ver
     put(&index_cap, 8);
     put(&results, sizeof results);
     put(&totals, sizeof totals);
-    put(&g_batch_chunk, 4);
-    put(&g_batch_block, 4);
-    put(&g_batch_brick_min_res, 4);
+    put(&b->tune, sizeof b->tune);
     cudaStream_t st = (cudaStream_t)stream;
     if (!b->exec || memcmp(key, b->graph_key, sizeof key) != 0) {
         if (b->exec) {
@@ -523,6 +590,83 @@ cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* ver
         memcpy(b->graph_key, key, sizeof key);
     }
     CG_CUDA(cudaGraphLaunch(b->exec, st));
+    return CG_OK;
+}
+
+cg_status cg_batch_autotune(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
+                            uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                            cg_job_mesh* results, uint32_t* totals, void* stream, uint32_t reps,
+                            cg_batch_tuning* best, float* best_ms) {
+    if (!b || !shape || reps < 1 || reps > 100) {
+        set_error("bad arguments to cg_batch_autotune");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceScope g(b->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CG_CUDA(cudaEventCreate(&e0));
+    cg_status rs = cuda_status(cudaEventCreate(&e1), "cudaEventCreate", __FILE__, __LINE__);
+    // Best of `reps` timed runs after one untimed run.
+    auto time_it = [&](const cg_batch_tuning& t, float* ms) -> cg_status {
+        b->tune = t;
+        CG_TRY(sync_plan(b));
+        CG_TRY(cg_batch_mesh(b, shape, vertices, vertex_cap, indices, index_cap, results, totals,
+                             st));
+        float lo = 3.4e38f;
+        for (uint32_t r = 0; r < reps; ++r) {
+            CG_CUDA(cudaEventRecord(e0, st));
+            CG_TRY(cg_batch_mesh(b, shape, vertices, vertex_cap, indices, index_cap, results,
+                                 totals, st));
+            CG_CUDA(cudaEventRecord(e1, st));
+            CG_CUDA(cudaEventSynchronize(e1));
+            float v = 0.0f;
+            CG_CUDA(cudaEventElapsedTime(&v, e0, e1));
+            lo = std::min(lo, v);
+        }
+        *ms = lo;
+        return CG_OK;
+    };
+    static const uint32_t kBrick[] = {8, 16, 32, 64, 1u << 20};
+    static const uint32_t kDeBlock[] = {128, 256, 512};
+    static const uint32_t kChunk[] = {4, 16, 64, 256};
+    static const uint32_t kPlace[] = {64, 128, 256};
+    cg_batch_tuning cur = b->tune;
+    float cur_ms = 0.0f;
+    if (rs == CG_OK) rs = time_it(cur, &cur_ms);
+    // Coordinate descent: each knob over its candidates with the others
+    // fixed, until a full pass changes nothing (at most three passes).
+    for (int pass = 0; pass < 3 && rs == CG_OK; ++pass) {
+        bool moved = false;
+        for (int knob = 0; knob < 4 && rs == CG_OK; ++knob) {
+            const uint32_t* vals = knob == 0 ? kBrick : knob == 1 ? kDeBlock : knob == 2 ? kChunk
+                                                                                      : kPlace;
+            const int nv = knob == 0 ? 5 : knob == 2 ? 4 : 3;
+            for (int i = 0; i < nv && rs == CG_OK; ++i) {
+                cg_batch_tuning t = cur;
+                uint32_t* field = knob == 0 ? &t.brick_min_res : knob == 1 ? &t.de_block
+                                                 : knob == 2 ? &t.de_chunk : &t.place_block;
+                if (*field == vals[i]) continue;
+                *field = vals[i];
+                float ms = 0.0f;
+                rs = time_it(t, &ms);
+                if (rs == CG_OK && ms < 0.97f * cur_ms) {  // 3% to beat timing noise
+                    cur = t;
+                    cur_ms = ms;
+                    moved = true;
+                }
+            }
+        }
+        if (!moved) break;
+    }
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    b->tune = cur;
+    const cg_status ps = sync_plan(b);
+    if (rs != CG_OK) return rs;
+    if (ps != CG_OK) return ps;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
     return CG_OK;
 }
 

@@ -233,6 +233,40 @@ cg_status cg_batch_mesh_graph(cg_batch* batch, const cg_shape* shape, cg_vertex*
 /* Device pointer of job `job`'s corner distances after a cg_batch_mesh. */
 cg_status cg_batch_dists(cg_batch* batch, uint32_t job, const float** dists);
 
+/* Launch shapes of one batch (no reference counterpart: the reference's
+ * thread pool has no such knobs).  None of them changes any output bit.
+ *   de_block       threads per block of the persistent step-1 kernel
+ *                  (power of two, 64..512; the grid is every block that fits
+ *                  on the GPU at once)
+ *   de_chunk       step-1 work items a warp takes from the queue per grab
+ *                  (1..4096)
+ *   brick_min_res  spans with resolution >= this are walked in 2x4x4 corner
+ *                  bricks per warp, smaller ones in runs of 32 corners
+ *   place_block    threads per block of vertex placement (64, 128, 256) */
+typedef struct cg_batch_tuning {
+    uint32_t de_block;
+    uint32_t de_chunk;
+    uint32_t brick_min_res;
+    uint32_t place_block;
+} cg_batch_tuning;
+
+cg_status cg_batch_get_tuning(const cg_batch* batch, cg_batch_tuning* tuning);
+/* Validates (CG_EINVAL) and applies; re-uploads the span table when
+ * brick_min_res changes (synchronous).  Not during a cg_batch_mesh capture. */
+cg_status cg_batch_set_tuning(cg_batch* batch, const cg_batch_tuning* tuning);
+
+/* The batch's autotuner: times cg_batch_mesh with these arguments (one
+ * untimed run, then the best of `reps` runs, CUDA events on `stream`) over
+ * candidate launch shapes by coordinate descent -- brick_min_res in
+ * {8, 16, 32, 64, never}, de_block in {128, 256, 512}, de_chunk in
+ * {4, 16, 64, 256}, place_block in {64, 128, 256} -- keeps a change only if
+ * it is 3% faster, applies the winner to the batch and returns it with its
+ * time.  Synchronous; the outputs hold a valid mesh afterwards. */
+cg_status cg_batch_autotune(cg_batch* batch, const cg_shape* shape, cg_vertex* vertices,
+                            uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
+                            cg_job_mesh* results, uint32_t* totals, void* stream, uint32_t reps,
+                            cg_batch_tuning* best, float* best_ms);
+
 /* ---- sphere tracing ----------------------------------------------------- */
 
 /* March loop of ShapeMesh::get_focii (src/mesh/mod.rs:229-241): for each ray
@@ -280,6 +314,14 @@ cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, cons
 cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, float* out,
                      void* stream);
 
+/* The same derivatives in forward (tangent) mode: one pass carries d/dq
+ * along x, y, z (and, with with_power != 0, d/dpower) next to the iterate,
+ * so there is no recompute.  Same out layout as cg_de_grad; with
+ * with_power == 0, out[4] (dDE/dpower) is 0 and the rest is computed.  Any
+ * max_iters >= 1.  No reference counterpart. */
+cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
+                             uint32_t with_power, float* out, void* stream);
+
 /* Backward of DE over a batch (the autograd.Function backward): given the
  * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to
  * grad_points (device n x 3, may be NULL) and the sums over i of
@@ -298,7 +340,9 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
 /* Process-wide tuning knobs.  "de_grid_kernel": 0 auto, 1 one corner per
  * thread in GridTable order, 2 one 2x4x4 brick per warp, 3 (P=8 only) one
  * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic.
- * All variants give bit-identical results. */
+ * All variants give bit-identical results.  "batch_block", "batch_chunk",
+ * "batch_brick_min_res", "batch_place_block": the cg_batch_tuning that
+ * batches created afterwards start with (defaults 256, 64, 32, 128). */
 cg_status cg_set_option(const char* name, int64_t value);
 
 /* The cudaStream_t (as void*) the mesher launches on, so a caller can time

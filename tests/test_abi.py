@@ -70,3 +70,34 @@ def test_no_device_does_not_crash(lib_path):
     h = C.c_void_p()
     st = L.cg_mesher_create(0, C.byref(h))
     assert st in (_ffi.CG_ENODEV, _ffi.CG_ECUDA)
+
+
+def test_ctypes_structs_match_header(tmp_path):
+    """sizeof / offsetof of every struct in the header, compiled by the C
+    compiler, equal the ctypes mirrors field by field."""
+    from cantucci_gb300 import _ffi
+    pairs = {"cg_shape": _ffi.CgShape, "cg_span": _ffi.CgSpan, "cg_timings": _ffi.CgTimings,
+             "cg_span_job": _ffi.CgSpanJob, "cg_job_mesh": _ffi.CgJobMesh,
+             "cg_camera": _ffi.CgCamera, "cg_batch_tuning": _ffi.CgBatchTuning}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "cantucci_gpu.h"',
+             'int main(void) {']
+    for cname, cls in pairs.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append('printf("cg_vertex %zu\\n", sizeof(cg_vertex)); return 0; }')
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe)], capture_output=True, text=True)
+    if r.returncode != 0 and "No such file" in r.stderr + r.stdout and "gcc" in r.stderr:
+        pytest.skip("no C compiler")
+    assert r.returncode == 0, r.stderr
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True,
+                                                   text=True).stdout.splitlines())
+    for cname, cls in pairs.items():
+        assert int(got[cname]) == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert int(got["%s.%s" % (cname, f)]) == getattr(cls, f).offset, (cname, f)
+    assert int(got["cg_vertex"]) == _ffi.VERTEX_DTYPE.itemsize == 28

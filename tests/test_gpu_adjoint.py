@@ -157,3 +157,69 @@ def test_adjoint_rejects_other_shapes(cg):
     out = torch.empty((4, 8), device="cuda")
     assert _ffi.load().cg_de_grad(C.byref(s), C.c_void_p(pts.data_ptr()), 4,
                                   C.c_void_p(out.data_ptr()), None) == _ffi.CG_EINVAL
+
+
+def test_tangent_mode_matches_adjoint(cg, orc):
+    """Forward mode linearises the same f32 trajectory as the adjoint: the
+    two agree far more tightly than either agrees with FP64."""
+    from cantucci_gb300.autograd import de_grad
+    rot = (0.2, 0.1, 0.0)
+    pts = band_points(cg, 4000, 8.3, rot, seed=8)
+    a = de_grad(pts, 8.3, rot).cpu().numpy().astype(np.float64)
+    t = de_grad(pts, 8.3, rot, mode="tangent").cpu().numpy().astype(np.float64)
+    # the DE column is the forward estimator's, bit for bit
+    d = cg.MandelbulbPolar(8.3, 15, 2.5, rot).batch_min_distance_from(pts).cpu().numpy()
+    np.testing.assert_array_equal(d.view(np.uint32), t[:, 0].astype(np.float32).view(np.uint32))
+    fin = np.all(np.isfinite(a), axis=1) & np.all(np.isfinite(t), axis=1)
+    assert fin.mean() > 0.99
+    ang = angle_deg(t[fin, 1:4], a[fin, 1:4])
+    assert np.mean(ang < 0.01) >= 0.99, np.quantile(ang, [0.5, 0.99])
+    rel = np.abs(t[fin, 4:8] - a[fin, 4:8]) / np.maximum(
+        np.linalg.norm(a[fin, 4:8], axis=1, keepdims=True), 1e-6)
+    assert np.mean(np.all(rel < 1e-3, axis=1)) >= 0.99, np.quantile(rel.max(1), [0.5, 0.99])
+    # against FP64 forward mode, the same bar as the adjoint
+    ref = orc.de_grad_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), pts.cpu().numpy())
+    ok = fin & np.all(np.isfinite(ref), axis=1)
+    ang64 = angle_deg(t[ok, 1:4], ref[ok, 1:4])
+    assert np.median(ang64) < 0.01 and np.mean(ang64 < 0.1) >= 0.9
+
+
+def test_tangent_mode_away_from_surface(cg, orc):
+    import torch
+    from cantucci_gb300.autograd import de_grad
+    rot = (0.2, 0.1, 0.0)
+    shape = cg.MandelbulbPolar(8.3, 15, 2.5, rot)
+    p = torch.as_tensor(W.uniform_points(200_000, seed=22)).cuda()
+    d = shape.batch_min_distance_from(p)
+    p = p[(d > 0.02) & (d < 0.3)][:3000].contiguous()
+    g = de_grad(p, 8.3, rot, mode="tangent").cpu().numpy().astype(np.float64)
+    ref = orc.de_grad_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), p.cpu().numpy())
+    ang = angle_deg(g[:, 1:4], ref[:, 1:4])
+    assert np.mean(ang < 0.01) >= 0.99, np.quantile(ang, [0.5, 0.99])
+    rel = np.abs(g[:, 4:8] - ref[:, 4:8]) / np.maximum(np.abs(ref[:, 4:8]), 1e-4)
+    assert np.mean(np.all(rel < 1e-3, axis=1)) >= 0.99, np.quantile(rel, 0.99, axis=0)
+
+
+def test_tangent_mode_without_power(cg):
+    from cantucci_gb300.autograd import de_grad
+    rot = (0.2, 0.1, 0.0)
+    pts = band_points(cg, 2000, 8.3, rot, seed=9)
+    full = de_grad(pts, 8.3, rot, mode="tangent").cpu().numpy()
+    pt = de_grad(pts, 8.3, rot, mode="tangent", with_power=False).cpu().numpy()
+    assert np.all(pt[:, 4] == 0)
+    np.testing.assert_array_equal(pt[:, 0].view(np.uint32), full[:, 0].view(np.uint32))
+    cols = [1, 2, 3, 5, 6, 7]
+    scale = np.maximum(np.linalg.norm(full[:, 1:4], axis=1, keepdims=True), 1e-6)
+    err = np.abs(pt[:, cols] - full[:, cols]) / scale
+    assert np.nanmax(err) < 1e-5
+
+
+def test_tangent_mode_any_max_iters(cg, orc):
+    """Forward mode has no checkpoint table, so max_iters above the
+    adjoint's 64 works."""
+    import torch
+    from cantucci_gb300.autograd import de_grad
+    p = torch.as_tensor(W.uniform_points(2000, seed=23)).cuda()
+    g = de_grad(p, 8.0, max_iters=80, mode="tangent").cpu().numpy().astype(np.float64)
+    d = cg.MandelbulbPolar(8.0, 80, 2.5).batch_min_distance_from(p).cpu().numpy()
+    np.testing.assert_array_equal(d.view(np.uint32), g[:, 0].astype(np.float32).view(np.uint32))

@@ -118,3 +118,60 @@ def test_batch_rejects_bad_job(cg):
     with pytest.raises(cg.CantucciError) as e:
         BatchMesher(spans, [8, 8])
     assert "job 1" in str(e.value)
+
+
+def test_tuning_changes_no_output_bit(cg):
+    """Every launch shape the autotuner can pick meshes the same bits."""
+    from cantucci_gb300.batch import BatchMesher
+    spans, res, _, _ = W.batched_spans(64, seed=5)
+    shape = cg.Mandelbulb(8, 15, 2.5)
+    b = BatchMesher(spans, res)
+    base = b.run(shape)
+    ref = [base.mesh(j) for j in range(len(res))]
+    for knobs in [dict(brick_min_res=8), dict(brick_min_res=1 << 20), dict(de_block=512),
+                  dict(de_block=128, de_chunk=1), dict(de_chunk=4096), dict(place_block=256),
+                  dict(place_block=64)]:
+        b.set_tuning(**knobs)
+        for graph in (False, True):
+            out = b.run(shape, graph=graph)
+            out._host = None
+            for j in range(len(res)):
+                v, i = out.mesh(j)
+                assert np.array_equal(i, ref[j][1]), (knobs, j)
+                assert np.array_equal(v.view(np.uint32), ref[j][0].view(np.uint32)), (knobs, j)
+    b.close()
+
+
+def test_autotune_applies_and_caches(cg, tmp_path):
+    from cantucci_gb300.batch import BatchMesher
+    spans, res, _, _ = W.batched_spans(256, seed=6)
+    shape = cg.Mandelbulb(8, 15, 2.5)
+    b = BatchMesher(spans, res)
+    ref = b.run(shape)
+    ref = [ref.mesh(j) for j in range(len(res))]
+    cache = str(tmp_path / "tune.json")
+    r = b.autotune(shape, reps=2, cache_path=cache)
+    assert not r["cached"] and r["ms"] > 0
+    assert b.tuning == r["tuning"]
+    out = b.run(shape, graph=True)
+    for j in range(len(res)):
+        v, i = out.mesh(j)
+        assert np.array_equal(i, ref[j][1])
+        assert np.array_equal(v.view(np.uint32), ref[j][0].view(np.uint32))
+    b2 = BatchMesher(spans, res)
+    r2 = b2.autotune(shape, cache_path=cache)
+    assert r2["cached"] and b2.tuning == r["tuning"]
+    b.close()
+    b2.close()
+
+
+def test_tuning_rejects_bad_values(cg):
+    from cantucci_gb300 import CantucciError
+    from cantucci_gb300.batch import BatchMesher
+    spans, res, _, _ = W.batched_spans(4, seed=7)
+    b = BatchMesher(spans, res)
+    for knobs in [dict(de_block=96), dict(de_block=1024), dict(de_chunk=0),
+                  dict(de_chunk=5000), dict(brick_min_res=1), dict(place_block=512)]:
+        with pytest.raises(CantucciError):
+            b.set_tuning(**knobs)
+    b.close()
