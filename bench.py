@@ -356,9 +356,80 @@ def extra_depth_fit(dev, steps=300):
             "loss_first": losses[0], "loss_last": losses[-1]}
 
 
+def extra_de_variants(dev, res=RES):
+    """The step-1 DE alone (cg_de_span_grid, no sign words) on the 513^3
+    span in three numerics: the exact P=8 polynomial (bit-faithful), the
+    same polynomial FMA-contracted with approximate division and square root
+    (not bit-faithful), and the real-power polar form at power 8.0 (the
+    reference's GLSL estimator, transcendental-bound).  Flop rates use the
+    exact path's algorithmic count (76 per iteration, the exact path's
+    iteration totals) for both P=8 variants."""
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import _ffi, workloads as W
+    lib = _ffi.load()
+    span = cg.Span(*W.SPAN_C1)
+    n = res + 1
+    out = torch.empty((n, n, n), dtype=torch.float32, device=dev)
+    exact = cg.Mandelbulb(**SHAPE)
+    steps_c, esc_c = C.c_uint64(), C.c_uint64()
+    _ffi.check(lib.cg_span_grid_work(C.byref(exact._cshape()), C.byref(span.to_c()), res,
+                                     C.byref(steps_c), C.byref(esc_c)))
+    flops = FLOPS_PER_STEP * steps_c.value + FLOPS_PER_ESCAPE * esc_c.value + FLOPS_PER_POINT * n ** 3
+    peak = C.c_double()
+    _ffi.check(lib.cg_fp32_peak_probe(20000, 0, C.byref(peak)))
+    res_out = {"workload": "%d^3 corners of [-1.2,1.2]^3 widened, max_iters 15" % n,
+               "fp32_peak_tflops": peak.value / 1e12}
+    for name, shape in (("exact_p8", exact), ("fast_p8", exact.fast()),
+                        ("polar_p8.0", cg.MandelbulbPolar(8.0, 15, 2.5))):
+        ms = _time_cuda(lambda: shape.span_grid(span, res, out=out), reps=5, warm=2)
+        e = {"ms": ms, "pts_per_s": n ** 3 / (ms * 1e-3)}
+        if name != "polar_p8.0":
+            e["tflops"] = flops / (ms * 1e-3) / 1e12
+            e["frac_of_fp32_peak"] = e["tflops"] * 1e12 / peak.value
+        res_out[name] = e
+    return res_out
+
+
+def extra_polar_mesh_normals(dev, res=RES):
+    """The span mesher on the polar Mandelbulb (power 8.0, max_iters 15) at
+    513^3 corners with the reference's six-sample normals and with analytic
+    (forward-mode) normals: same vertices, DE values and indices; step 2
+    time compared."""
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    span = cg.Span(*W.SPAN_C1)
+    shape = cg.MandelbulbPolar(8.0, 15, 2.5)
+    vcap, icap = res ** 3 // 16, 18 * res ** 3 // 16
+    v = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(icap, dtype=torch.int32, device=dev)
+    out = {"workload": "polar Mandelbulb power 8.0, max_iters 15, %d^3 corners" % (res + 1)}
+    m = cg.Mesher(dev)
+    try:
+        for mode in ("fd", "analytic"):
+            m.set_normals(mode)
+            m.generate_device(span, shape, res, v, i, strict=False)
+            tms = []
+            for _ in range(3):
+                nv, ni, tm = m.generate_device(span, shape, res, v, i, strict=False)
+                tms.append(tm)
+            out[mode] = {"step1_ms": min(t.first_ms for t in tms),
+                         "step2_ms": min(t.second_ms for t in tms),
+                         "step3_ms": min(t.third_ms for t in tms),
+                         "mesh_ms": min(t.first_ms + t.second_ms + t.third_ms for t in tms),
+                         "vertices": nv, "indices": ni}
+    finally:
+        m.close()
+    out["step2_speedup"] = out["fd"]["step2_ms"] / out["analytic"]["step2_ms"]
+    out["mesh_speedup"] = out["fd"]["mesh_ms"] / out["analytic"]["mesh_ms"]
+    return out
+
+
 def run_extras(args, dev):
     out = {}
-    for name, fn in (("batched_spans", extra_batched), ("normals", extra_normals),
+    for name, fn in (("de_variants", extra_de_variants), ("batched_spans", extra_batched),
+                     ("normals", extra_normals), ("polar_mesh_normals", extra_polar_mesh_normals),
                      ("depth_fit", extra_depth_fit)):
         try:
             out[name] = fn(dev)

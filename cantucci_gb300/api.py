@@ -263,6 +263,13 @@ class Mesher:
         except Exception:
             pass
 
+    def set_normals(self, mode: str):
+        """"fd": the reference's six-sample central difference (default);
+        "analytic": the forward-mode gradient, one pass per vertex (polar
+        Mandelbulb only)."""
+        modes = {"fd": _ffi.CG_NORMALS_FD, "analytic": _ffi.CG_NORMALS_ADJOINT}
+        check(self._lib.cg_mesher_set_normals(self.handle, modes[mode]))
+
     def generate(self, span: Span, shape: Shape, resolution: int, vertex_cap=None,
                  index_cap=None, vertices=None, indices=None, strict: bool = True):
         """Mesh into host numpy arrays (pinned torch tensors also accepted).

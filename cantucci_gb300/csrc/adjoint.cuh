@@ -1,6 +1,8 @@
 // adjoint.cuh -- reverse-mode gradient of the real-power polar estimator
 // (src/shape/mandelbulb.frag:1-39, rotated), shared by the point kernels
-// (adjoint.cu) and the depth-map backward (trace.cu).
+// (adjoint.cu) and the depth-map backward (trace.cu); and its forward-mode
+// twin polar_de_tangent (end of file), also used for analytic mesh normals
+// (mesh_rows.cuh).
 //
 // For the polar loop one thread returns, per point,
 //   DE, dDE/dp (3), dDE/dpower, dDE/d(euler angles) (3).
@@ -220,7 +222,7 @@ __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __
 // the three point directions).  Work: one forward pass plus T tangent
 // updates of ~30 operations per step, against polar_de_grad's two forward
 // passes plus one backward step.
-template <int T>
+template <int T, bool Rot = true>
 __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float* __restrict__ dm,
                                                  float px, float py, float pz, float* out) {
     const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
@@ -303,6 +305,7 @@ __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float*
     out[2] = s.m[3] * g[0] + s.m[4] * g[1] + s.m[5] * g[2];
     out[3] = s.m[6] * g[0] + s.m[7] * g[1] + s.m[8] * g[2];
     out[4] = g[3];
+    if (!Rot) return;  // out[0..4] only (dm unused)
     for (int a = 0; a < 3; ++a) {
         const float* d = dm + 9 * a;
         const float dqx = d[0] * px + d[3] * py + d[6] * pz;

@@ -187,6 +187,10 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
                    cg_timings* tm) {
     CG_TRY(check_span_res(span, res));
     CG_TRY(check_shape(shape));
+    if (m->normals == CG_NORMALS_ADJOINT && shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
+        set_error("analytic normals are built for the polar Mandelbulb (kind 2) only");
+        return CG_EINVAL;
+    }
     const ShapeDev s = make_shape_dev(*shape);
     const SpanSetup su = setup_span(*span, res);
     const MeshDims d = mesh_dims(res);
@@ -200,7 +204,8 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
-                                  /*signs_ready=*/true));
+                                  /*signs_ready=*/true,
+                                  /*analytic_normals=*/m->normals == CG_NORMALS_ADJOINT));
     CG_CUDA(cudaEventRecord(m->ev[3], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -338,10 +343,6 @@ void cg_mesher_destroy(cg_mesher* m) {
 cg_status cg_mesher_set_normals(cg_mesher* m, uint32_t normals) {
     if (!m || normals > CG_NORMALS_ADJOINT) {
         set_error("bad mesher or normals mode");
-        return CG_EINVAL;
-    }
-    if (normals != CG_NORMALS_FD) {
-        set_error("adjoint normals are not built into this mesher");
         return CG_EINVAL;
     }
     std::lock_guard<std::mutex> lk(m->mu);

@@ -83,11 +83,13 @@ size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 
 // Steps 2 and 3 of naive_surface_nets on a filled `dists` grid (and, with
 // signs_ready, filled sign words).  Output arrays are written only up to
-// their capacity; counts land in w.counters.
+// their capacity; counts land in w.counters.  analytic_normals (polar form
+// only) replaces the six-sample normal by the forward-mode gradient.
 cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
-                                 cudaEvent_t ev_after_vertices, bool signs_ready);
+                                 cudaEvent_t ev_after_vertices, bool signs_ready,
+                                 bool analytic_normals = false);
 
 // Cell -> vertex id table of the last mesh (0xFFFFFFFF off the surface).
 cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* points,

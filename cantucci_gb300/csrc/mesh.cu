@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
 }
 
 // One vertex per thread (buffer.rs:149-274).
-template <int M>
+template <int M, bool AN>
 __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshDims d,
                                                const float* __restrict__ dists,
                                                const uint32_t* __restrict__ cellidx,
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
     bool bad = false;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         float* o = v < vcap ? reinterpret_cast<float*>(verts + v) : nullptr;
-        bad |= !place_vertex<M>(s, pp, d, dists, cellidx[v], o);
+        bad |= !place_vertex<M, AN>(s, pp, d, dists, cellidx[v], o);
     }
     if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
 }
@@ -160,7 +160,8 @@ PlaceParams place_params(const SpanSetup& su) {
 cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
-                                 cudaEvent_t ev_after_vertices, bool signs_ready) {
+                                 cudaEvent_t ev_after_vertices, bool signs_ready,
+                                 bool analytic_normals) {
     const uint32_t rows = d.res * d.res;
     CG_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(MeshCounters), st));
     if (!signs_ready) {
@@ -186,17 +187,21 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
         const unsigned G = (unsigned)sm_count() * 16;
         switch (mode_of(s, CG_NUMERICS_EXACT)) {
         case MODE_P8:
-            k_place<MODE_P8><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
+            k_place<MODE_P8, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
             break;
         case MODE_INT:
-            k_place<MODE_INT><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
+            k_place<MODE_INT, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
             break;
         case MODE_POLAR:
-            k_place<MODE_POLAR><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                                 vcap);
+            if (analytic_normals)
+                k_place<MODE_POLAR, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx,
+                                                           w.counters, verts, vcap);
+            else
+                k_place<MODE_POLAR, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx,
+                                                            w.counters, verts, vcap);
             break;
         default:
-            k_place<MODE_SPHERE><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
+            k_place<MODE_SPHERE, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
                                                   vcap);
             break;
         }

@@ -16,6 +16,7 @@
 
 #include <cstdint>
 
+#include "adjoint.cuh"
 #include "de.cuh"
 #include "kernels.cuh"
 
@@ -88,8 +89,11 @@ PlaceParams place_params(const SpanSetup& su);
 
 // Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
 // crossings, DE at the vertex and the six-sample central-difference normal.
+// With AN (polar form only) the normal is instead the normalised analytic
+// gradient from one forward-mode pass, which also gives the DE at the vertex
+// (the same bits as the estimator's).
 // Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
-template <int M>
+template <int M, bool AN = false>
 __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
                                              const MeshDims& d, const float* __restrict__ dists,
                                              uint32_t c, float* __restrict__ o) {
@@ -155,6 +159,21 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
     // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
     // loop is kept rolled so that one copy of the estimator is in the code.
     float de[7];
+    if (AN) {
+        float g[5];
+        polar_de_tangent<3, false>(s, nullptr, vx, vy, vz, g);
+        const float inv = __fdiv_rn(1.0f, magnitude<Exact>(g[1], g[2], g[3]));
+        if (o) {
+            o[0] = vx;
+            o[1] = vy;
+            o[2] = vz;
+            o[3] = __fmul_rn(g[1], inv);
+            o[4] = __fmul_rn(g[2], inv);
+            o[5] = __fmul_rn(g[3], inv);
+            o[6] = g[0];
+        }
+        return !bad;
+    }
 #pragma unroll 1
     for (int k = 0; k < 7; ++k) {
         float qx = vx, qy = vy, qz = vz;

@@ -120,7 +120,7 @@ def fit(target, cam, power0=8.0, rot0=(0.0, 0.0, 0.0), steps=300, lr=1e-2, max_s
         loss = l1_loss(depth, target)
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
         if callback:
             callback(it, float(power), rot.detach().tolist(), losses[-1])
     return float(power), rot.detach().tolist(), losses

@@ -55,7 +55,8 @@ enum {
 /* Normals of the mesher. */
 enum {
     CG_NORMALS_FD = 0,      /* six central differences, as buffer.rs:256-266 */
-    CG_NORMALS_ADJOINT = 1  /* analytic dDE/dp from the adjoint kernel (new) */
+    CG_NORMALS_ADJOINT = 1  /* analytic dDE/dp, one forward-mode pass per vertex instead of
+                               six extra estimator calls; polar Mandelbulb only (new) */
 };
 
 /* A shape; 48 bytes.  `power`/`max_iters`/`bailout` are Mandelbulb's fields
@@ -136,7 +137,10 @@ typedef struct cg_mesher cg_mesher;
 /* A mesher owns a stream, events and a grow-only device workspace. */
 cg_status cg_mesher_create(int device, cg_mesher** out);
 void cg_mesher_destroy(cg_mesher* mesher);
-/* Select the normals (CG_NORMALS_FD default). */
+/* Select the normals (CG_NORMALS_FD default).  With CG_NORMALS_ADJOINT a
+ * mesh of any shape but the polar Mandelbulb fails with CG_EINVAL; vertex
+ * positions, DE values and indices are unchanged, only the normals differ
+ * from the reference's six-sample difference. */
 cg_status cg_mesher_set_normals(cg_mesher* mesher, uint32_t normals);
 
 /* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.

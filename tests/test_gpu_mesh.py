@@ -197,3 +197,32 @@ def test_c2_full_size_vs_oracle(cg, orc, mesher):
     a, b = as7(verts[:nv]), as7(ref["vertices"])
     np.testing.assert_allclose(a[:, :3], b[:, :3], rtol=0, atol=1e-6)
     assert n == gpu_points.size
+
+
+def test_analytic_normals(cg, orc):
+    """Analytic (forward-mode) normals: the same mesh except the normals,
+    which match the FP64 gradient at the vertex."""
+    rot = (0.2, 0.1, 0.0)
+    shape = cg.MandelbulbPolar(8.3, 15, 2.5, rot)
+    span = cg.Span(*W.SPAN_C1)
+    m = cg.Mesher(0)
+    try:
+        v0, i0, nv0, ni0, _ = m.generate(span, shape, 64)
+        m.set_normals("analytic")
+        v1, i1, nv1, ni1, _ = m.generate(span, shape, 64)
+        with pytest.raises(cg.CantucciError):
+            m.generate(span, cg.Mandelbulb(8, 15, 2.5), 16)
+    finally:
+        m.close()
+    assert (nv0, ni0) == (nv1, ni1) and nv0 > 1000
+    a, b = as7(v0[:nv0]), as7(v1[:nv1])
+    assert np.array_equal(i0[:ni0], i1[:ni1])
+    assert np.array_equal(a[:, [0, 1, 2, 6]].view(np.uint32), b[:, [0, 1, 2, 6]].view(np.uint32))
+    g = orc.de_grad_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), b[:, :3])
+    ok = np.all(np.isfinite(g[:, 1:4]), axis=1) & np.all(np.isfinite(b[:, 3:6]), axis=1)
+    assert ok.mean() > 0.99
+    ang = angle_deg(b[ok, 3:6], g[ok, 1:4])
+    assert np.median(ang) < 0.01 and np.mean(ang < 0.1) >= 0.9, np.quantile(ang, [0.5, 0.9])
+    # the six-sample normal is much further from the gradient
+    ang_fd = angle_deg(a[ok, 3:6], g[ok, 1:4])
+    assert np.median(ang_fd) > np.median(ang)
