@@ -56,6 +56,25 @@ class CgJobMesh(C.Structure):
                 ("vertices", C.c_uint32), ("indices", C.c_uint32)]
 
 
+class CgView(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("fov_y", C.c_float),
+                ("aspect", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float)]
+
+
+class CgLodStats(C.Structure):
+    _fields_ = [("focii", C.c_uint32), ("splits", C.c_uint32), ("collected", C.c_uint32),
+                ("started", C.c_uint32), ("active", C.c_uint32), ("leaves", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class CgLeaf(C.Structure):
+    _fields_ = [("span", CgSpan), ("status", C.c_uint32), ("depth", C.c_uint32),
+                ("vertices", C.c_void_p), ("indices", C.c_void_p), ("n_vertices", C.c_uint32),
+                ("n_indices", C.c_uint32)]
+
+
 class CgBatchTuning(C.Structure):
     _fields_ = [("de_block", C.c_uint32), ("de_chunk", C.c_uint32),
                 ("brick_min_res", C.c_uint32), ("place_block", C.c_uint32)]
@@ -94,6 +113,13 @@ SIGNATURES = [
     ("cg_batch_mesh", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_mesh_graph", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp]),
     ("cg_batch_dists", _i32, [_vp, _u32, C.POINTER(_vp)]),
+    ("cg_batch_set_jobs", _i32, [_vp, _vp, _u32]),
+    ("cg_view_focus_rays", _i32, [C.POINTER(CgView), _u32, _vp, _vp]),
+    ("cg_shape_mesh_create", _i32, [_i32, _shp, _spp, _u32, C.POINTER(_vp)]),
+    ("cg_shape_mesh_destroy", None, [_vp]),
+    ("cg_shape_mesh_update", _i32, [_vp, C.POINTER(CgView), _u32, C.POINTER(CgLodStats)]),
+    ("cg_shape_mesh_leaves", _i32, [_vp, C.POINTER(CgLeaf), _u32, C.POINTER(_u32)]),
+    ("cg_shape_mesh_focii", _i32, [_vp, _vp, _u32, C.POINTER(_u32)]),
     ("cg_batch_get_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
     ("cg_batch_set_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
     ("cg_batch_autotune", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp, _u32,

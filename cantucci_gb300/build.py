@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIB_DIR, "libcantucci_gpu.so")
 
 SOURCES = ["capi.cu", "de_kernels.cu", "mesh.cu", "mesh_batch.cu", "adjoint.cu", "trace.cu", "scan.cu",
-           "probe.cu", "noalloc.cu"]
+           "probe.cu", "noalloc.cu", "lod.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",

@@ -305,13 +305,14 @@ __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float*
     out[2] = s.m[3] * g[0] + s.m[4] * g[1] + s.m[5] * g[2];
     out[3] = s.m[6] * g[0] + s.m[7] * g[1] + s.m[8] * g[2];
     out[4] = g[3];
-    if (!Rot) return;  // out[0..4] only (dm unused)
-    for (int a = 0; a < 3; ++a) {
-        const float* d = dm + 9 * a;
-        const float dqx = d[0] * px + d[3] * py + d[6] * pz;
-        const float dqy = d[1] * px + d[4] * py + d[7] * pz;
-        const float dqz = d[2] * px + d[5] * py + d[8] * pz;
-        out[5 + a] = g[0] * dqx + g[1] * dqy + g[2] * dqz;
+    if constexpr (Rot) {  // without Rot: out[0..4] only (dm unused)
+        for (int a = 0; a < 3; ++a) {
+            const float* d = dm + 9 * a;
+            const float dqx = d[0] * px + d[3] * py + d[6] * pz;
+            const float dqy = d[1] * px + d[4] * py + d[7] * pz;
+            const float dqz = d[2] * px + d[5] * py + d[8] * pz;
+            out[5 + a] = g[0] * dqx + g[1] * dqy + g[2] * dqz;
+        }
     }
 }
 

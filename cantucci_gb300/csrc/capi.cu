@@ -85,7 +85,7 @@ GridDev make_grid(const SpanSetup& su, uint32_t res) {
     return g;
 }
 
-static cg_status check_shape(const cg_shape* s) {
+cg_status check_shape(const cg_shape* s) {
     if (!s) {
         set_error("shape is NULL");
         return CG_EINVAL;

@@ -256,6 +256,10 @@ struct cg_batch {
     size_t sgn_words = 0;
     std::vector<uint32_t> res;    // per job, host copy
     std::vector<BatchJob> hjobs;  // host copy of the span table
+    // workspace capacities (from creation): a new job list must fit them
+    uint32_t cap_jobs = 0;
+    uint64_t cap_dist = 0, cap_sgnw = 0, cap_cw = 0, cap_rows = 0;
+    uint32_t plan_gen = 0;  // bumped by cg_batch_set_jobs (graphs recapture)
     cg_batch_tuning tune = {256, 64, 32, 128};
     uint32_t planned_brick_min_res = 0;  // the threshold the device table holds
     // graph cache
@@ -297,6 +301,57 @@ cg_status plan_items(std::vector<BatchJob>& jobs, uint32_t brick_min_res, uint32
         }
     }
     *total = (uint32_t)items;
+    return CG_OK;
+}
+
+struct PlanTotals {
+    uint64_t dist = 0, sgnw = 0, cw = 0, rows = 0;
+};
+
+// The span table of a job list (everything but the step-1 items) and its
+// workspace totals; validates each job as generate_for_box does.
+cg_status build_jobs(const cg_span_job* host_jobs, uint32_t n_jobs, std::vector<BatchJob>& jobs,
+                     PlanTotals* t) {
+    jobs.assign(n_jobs, BatchJob{});
+    PlanTotals acc;
+    for (uint32_t i = 0; i < n_jobs; ++i) {
+        const cg_span_job& hj = host_jobs[i];
+        const uint32_t res = hj.resolution;
+        for (int k = 0; k < 3; ++k) {
+            if (!(hj.span.start[k] < hj.span.end[k])) {
+                set_error("job %u: span.start[%d] < span.end[%d] does not hold", i, k, k);
+                return CG_EINVAL;
+            }
+        }
+        if (res < 2 || (res & (res - 1)) || res > 1024) {
+            set_error("job %u: resolution %u must be a power of two in [2, 1024]", i, res);
+            return CG_EINVAL;
+        }
+        const SpanSetup su = setup_span(hj.span, res);
+        BatchJob& J = jobs[i];
+        memset(&J, 0, sizeof J);
+        for (int k = 0; k < 3; ++k) {
+            J.start[k] = su.start[k];
+            J.across[k] = su.across[k];
+        }
+        J.inv_res = 1.0f / (float)res;
+        J.pp = place_params(su);
+        J.d = mesh_dims(res);
+        const uint64_t n = J.d.n;
+        J.dist_off = acc.dist;
+        J.sgn_off = acc.sgnw;
+        J.cw_off = acc.cw;
+        J.row_begin = (uint32_t)acc.rows;
+        acc.dist += n * n * n;
+        acc.sgnw += n * n * J.d.W;
+        acc.cw += (uint64_t)res * res * J.d.Wc;
+        acc.rows += (uint64_t)res * res;
+        if (acc.rows > (16u << 20) || acc.dist > 0xFFFFFFFFull * 4) {
+            set_error("batch too large: %llu cell rows", (unsigned long long)acc.rows);
+            return CG_EINVAL;
+        }
+    }
+    *t = acc;
     return CG_OK;
 }
 
@@ -356,45 +411,10 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
         return CG_EINVAL;
     }
     *out = nullptr;
-    std::vector<BatchJob> jobs(n_jobs);
-    uint64_t dist = 0, sgnw = 0, cw = 0, rows = 0;
-    for (uint32_t i = 0; i < n_jobs; ++i) {
-        const cg_span_job& hj = host_jobs[i];
-        const uint32_t res = hj.resolution;
-        for (int k = 0; k < 3; ++k) {
-            if (!(hj.span.start[k] < hj.span.end[k])) {
-                set_error("job %u: span.start[%d] < span.end[%d] does not hold", i, k, k);
-                return CG_EINVAL;
-            }
-        }
-        if (res < 2 || (res & (res - 1)) || res > 1024) {
-            set_error("job %u: resolution %u must be a power of two in [2, 1024]", i, res);
-            return CG_EINVAL;
-        }
-        const SpanSetup su = setup_span(hj.span, res);
-        BatchJob& J = jobs[i];
-        memset(&J, 0, sizeof J);
-        for (int k = 0; k < 3; ++k) {
-            J.start[k] = su.start[k];
-            J.across[k] = su.across[k];
-        }
-        J.inv_res = 1.0f / (float)res;
-        J.pp = place_params(su);
-        J.d = mesh_dims(res);
-        const uint64_t n = J.d.n;
-        J.dist_off = dist;
-        J.sgn_off = sgnw;
-        J.cw_off = cw;
-        J.row_begin = (uint32_t)rows;
-        dist += n * n * n;
-        sgnw += n * n * J.d.W;
-        cw += (uint64_t)res * res * J.d.Wc;
-        rows += (uint64_t)res * res;
-        if (rows > (16u << 20) || dist > 0xFFFFFFFFull * 4) {
-            set_error("batch too large: %llu cell rows", (unsigned long long)rows);
-            return CG_EINVAL;
-        }
-    }
+    std::vector<BatchJob> jobs;
+    PlanTotals t;
+    CG_TRY(build_jobs(host_jobs, n_jobs, jobs, &t));
+    const uint64_t dist = t.dist, sgnw = t.sgnw, cw = t.cw, rows = t.rows;
     const cg_batch_tuning tune = g_batch_default;
     uint32_t items = 0;
     CG_TRY(plan_items(jobs, tune.brick_min_res, &items));
@@ -410,6 +430,11 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
     b->planned_brick_min_res = tune.brick_min_res;
     b->res.resize(n_jobs);
     for (uint32_t i = 0; i < n_jobs; ++i) b->res[i] = host_jobs[i].resolution;
+    b->cap_jobs = n_jobs;
+    b->cap_dist = dist;
+    b->cap_sgnw = sgnw;
+    b->cap_cw = cw;
+    b->cap_rows = rows;
     size_t off = 0;
     std::vector<std::pair<void**, size_t>> parts = {
         {(void**)&b->jobs, sizeof(BatchJob) * n_jobs},
@@ -457,6 +482,36 @@ void cg_batch_destroy(cg_batch* b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->work) cudaFree(b->work);
     delete b;
+}
+
+cg_status cg_batch_set_jobs(cg_batch* b, const cg_span_job* host_jobs, uint32_t n_jobs) {
+    if (!b || !host_jobs || n_jobs == 0) {
+        set_error("bad arguments to cg_batch_set_jobs");
+        return CG_EINVAL;
+    }
+    std::vector<BatchJob> jobs;
+    PlanTotals t;
+    CG_TRY(build_jobs(host_jobs, n_jobs, jobs, &t));
+    if (n_jobs > b->cap_jobs || t.dist > b->cap_dist || t.sgnw > b->cap_sgnw ||
+        t.cw > b->cap_cw || t.rows > b->cap_rows) {
+        set_error("job list does not fit the batch's workspace (create a larger batch)");
+        return CG_ECAPACITY;
+    }
+    uint32_t items = 0;
+    CG_TRY(plan_items(jobs, b->tune.brick_min_res, &items));
+    std::lock_guard<std::mutex> lk(b->mu);
+    DeviceScope g(b->device);
+    CG_CUDA(cudaMemcpy(b->jobs, jobs.data(), sizeof(BatchJob) * n_jobs, cudaMemcpyHostToDevice));
+    b->hjobs = std::move(jobs);
+    b->njobs = n_jobs;
+    b->total_items = items;
+    b->rows = (uint32_t)t.rows;
+    b->sgn_words = t.sgnw;
+    b->planned_brick_min_res = b->tune.brick_min_res;
+    b->res.assign(n_jobs, 0);
+    for (uint32_t i = 0; i < n_jobs; ++i) b->res[i] = host_jobs[i].resolution;
+    ++b->plan_gen;
+    return CG_OK;
 }
 
 cg_status cg_batch_get_tuning(const cg_batch* b, cg_batch_tuning* t) {
@@ -561,6 +616,7 @@ cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* ver
     put(&results, sizeof results);
     put(&totals, sizeof totals);
     put(&b->tune, sizeof b->tune);
+    put(&b->plan_gen, sizeof b->plan_gen);
     cudaStream_t st = (cudaStream_t)stream;
     if (!b->exec || memcmp(key, b->graph_key, sizeof key) != 0) {
         if (b->exec) {

@@ -158,8 +158,7 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
     // Sample 0 is the vertex; samples 1..6 are p + unit * (+-delta) along
     // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
     // loop is kept rolled so that one copy of the estimator is in the code.
-    float de[7];
-    if (AN) {
+    if constexpr (AN) {
         float g[5];
         polar_de_tangent<3, false>(s, nullptr, vx, vy, vz, g);
         const float inv = __fdiv_rn(1.0f, magnitude<Exact>(g[1], g[2], g[3]));
@@ -173,39 +172,41 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
             o[6] = g[0];
         }
         return !bad;
-    }
+    } else {
+        float de[7];
 #pragma unroll 1
-    for (int k = 0; k < 7; ++k) {
-        float qx = vx, qy = vy, qz = vz;
-        if (k > 0) {
-            const int axis = (k - 1) >> 1;
-            const bool neg = ((k - 1) & 1) != 0;
-            const float zero = neg ? -0.0f : 0.0f;
-            const float dd0 = axis == 0 ? pp.delta[0] : (axis == 1 ? pp.delta[1] : pp.delta[2]);
-            const float off = neg ? -dd0 : dd0;
-            qx = __fadd_rn(vx, axis == 0 ? off : zero);
-            qy = __fadd_rn(vy, axis == 1 ? off : zero);
-            qz = __fadd_rn(vz, axis == 2 ? off : zero);
-        }
-        const float val = eval<M>(s, qx, qy, qz);
+        for (int k = 0; k < 7; ++k) {
+            float qx = vx, qy = vy, qz = vz;
+            if (k > 0) {
+                const int axis = (k - 1) >> 1;
+                const bool neg = ((k - 1) & 1) != 0;
+                const float zero = neg ? -0.0f : 0.0f;
+                const float dd0 = axis == 0 ? pp.delta[0] : (axis == 1 ? pp.delta[1] : pp.delta[2]);
+                const float off = neg ? -dd0 : dd0;
+                qx = __fadd_rn(vx, axis == 0 ? off : zero);
+                qy = __fadd_rn(vy, axis == 1 ? off : zero);
+                qz = __fadd_rn(vz, axis == 2 ? off : zero);
+            }
+            const float val = eval<M>(s, qx, qy, qz);
 #pragma unroll
-        for (int j = 0; j < 7; ++j) de[j] = (j == k) ? val : de[j];
+            for (int j = 0; j < 7; ++j) de[j] = (j == k) ? val : de[j];
+        }
+        const float nx = __fsub_rn(de[1], de[2]);
+        const float ny = __fsub_rn(de[3], de[4]);
+        const float nz = __fsub_rn(de[5], de[6]);
+        // cgmath normalize: v * (1 / |v|), |v| = sqrt((x*x + y*y) + z*z).
+        const float inv = __fdiv_rn(1.0f, magnitude<Exact>(nx, ny, nz));
+        if (o) {
+            o[0] = vx;
+            o[1] = vy;
+            o[2] = vz;
+            o[3] = __fmul_rn(nx, inv);
+            o[4] = __fmul_rn(ny, inv);
+            o[5] = __fmul_rn(nz, inv);
+            o[6] = de[0];
+        }
+        return !bad;
     }
-    const float nx = __fsub_rn(de[1], de[2]);
-    const float ny = __fsub_rn(de[3], de[4]);
-    const float nz = __fsub_rn(de[5], de[6]);
-    // cgmath normalize: v * (1 / |v|), |v| = sqrt((x*x + y*y) + z*z).
-    const float inv = __fdiv_rn(1.0f, magnitude<Exact>(nx, ny, nz));
-    if (o) {
-        o[0] = vx;
-        o[1] = vy;
-        o[2] = vz;
-        o[3] = __fmul_rn(nx, inv);
-        o[4] = __fmul_rn(ny, inv);
-        o[5] = __fmul_rn(nz, inv);
-        o[6] = de[0];
-    }
-    return !bad;
 }
 
 // Edge crossings of the corners of one corner row, 32 corners per word

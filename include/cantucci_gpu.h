@@ -237,6 +237,14 @@ cg_status cg_batch_mesh_graph(cg_batch* batch, const cg_shape* shape, cg_vertex*
 /* Device pointer of job `job`'s corner distances after a cg_batch_mesh. */
 cg_status cg_batch_dists(cg_batch* batch, uint32_t job, const float** dists);
 
+/* Replaces the batch's job list without reallocating, for a caller that
+ * meshes a new set of leaves every frame (ShapeMesh::update's job fan-out,
+ * src/mesh/mod.rs:125-161).  The list must fit the workspace the batch was
+ * created with (no more jobs, corners, sign words, cell words or cell rows),
+ * else CG_ECAPACITY; jobs are validated like cg_batch_create's.  The batch
+ * must be idle (no cg_batch_mesh of it still running).  jobs: HOST. */
+cg_status cg_batch_set_jobs(cg_batch* batch, const cg_span_job* jobs, uint32_t n_jobs);
+
 /* Launch shapes of one batch (no reference counterpart: the reference's
  * thread pool has no such knobs).  None of them changes any output bit.
  *   de_block       threads per block of the persistent step-1 kernel
@@ -279,6 +287,85 @@ cg_status cg_batch_autotune(cg_batch* batch, const cg_shape* shape, cg_vertex* v
 cg_status cg_march(const cg_shape* shape, const float* origins, const float* dirs, uint64_t n,
                    uint32_t max_steps, float epsilon, float* hits, uint8_t* hit,
                    void* stream);
+
+/* ---- level of detail: ShapeMesh ------------------------------------------ */
+
+/* The camera of src/camera.rs:14-19,175-189: position, look direction
+ * (normalised by the callee), vertical field of view (radians), aspect ratio
+ * (width / height), near and far plane; up is (0, 0, 1). */
+typedef struct cg_view {
+    float position[3];
+    float direction[3];
+    float fov_y;
+    float aspect;
+    float near_plane;
+    float far_plane;
+} cg_view;
+
+/* The rays of ShapeMesh::get_focii (src/mesh/mod.rs:205-243): the centres
+ * of a focus_points x focus_points grid on the near plane (iter::square
+ * order: x outer, y inner, src/util/iter.rs:54-88), moved to world space by
+ * the inverse view transform; each ray starts at the camera position.
+ * Host arithmetic only (needs no GPU).  origins, dirs: HOST, n^2 x 3 floats. */
+cg_status cg_view_focus_rays(const cg_view* view, uint32_t focus_points, float* origins,
+                             float* dirs);
+
+typedef struct cg_shape_mesh cg_shape_mesh;
+
+/* ShapeMesh::new (src/mesh/mod.rs:45-78): an octree spanning `bounds` (the
+ * shape's bounding_box) with its first two levels split, i.e. 64 empty
+ * leaves; leaves are meshed at `resolution` (64 in the reference). */
+cg_status cg_shape_mesh_create(int device, const cg_shape* shape, const cg_span* bounds,
+                               uint32_t resolution, cg_shape_mesh** out);
+void cg_shape_mesh_destroy(cg_shape_mesh* sm);
+
+typedef struct cg_lod_stats {
+    uint32_t focii;      /* focus rays that hit the surface */
+    uint32_t splits;     /* ready leaves split by this update */
+    uint32_t collected;  /* meshes that became ready in this update */
+    uint32_t started;    /* mesh jobs started by this update */
+    uint32_t active;     /* jobs in flight after this update */
+    uint32_t leaves;     /* leaves of the octree after this update */
+} cg_lod_stats;
+
+/* ShapeMesh::update (src/mesh/mod.rs:82-178), in the reference's order:
+ * (1) the 5 x 5 focus rays are marched on the GPU (100 steps, hit when
+ *     DE < 1e-6) and every READY leaf around a hit closer to the camera than
+ *     twice the leaf's width is split into eight empty leaves;
+ * (2) if the previous update's jobs have finished (or, with wait != 0,
+ *     after waiting for them) their meshes become ready, each in the leaf
+ *     around its span's centre;
+ * (3) every empty leaf becomes a job: all of them are meshed by one batched
+ *     persistent launch chain (the thread pool's generate_for_box jobs),
+ *     asynchronously; those leaves are "requested" until a later update
+ *     collects them.
+ * stats may be NULL. */
+cg_status cg_shape_mesh_update(cg_shape_mesh* sm, const cg_view* view, uint32_t wait,
+                               cg_lod_stats* stats);
+
+/* A leaf of the octree.  status: 0 empty, 1 requested, 2 ready.  vertices /
+ * indices: DEVICE pointers to the leaf's mesh while ready (NULL otherwise),
+ * valid until the next cg_shape_mesh_update or destroy; its indices refer to
+ * its own vertices, as the leaf's MeshBuffer would. */
+typedef struct cg_leaf {
+    cg_span span;
+    uint32_t status;
+    uint32_t depth;
+    const cg_vertex* vertices;
+    const uint32_t* indices;
+    uint32_t n_vertices;
+    uint32_t n_indices;
+} cg_leaf;
+
+/* The leaves in the reference's traversal order (Octree::iter pops a stack
+ * and pushes children 0..7, src/octree/iter.rs:24-33).  Writes
+ * min(count, cap) entries; *count = the number of leaves.  leaves: HOST. */
+cg_status cg_shape_mesh_leaves(cg_shape_mesh* sm, cg_leaf* leaves, uint32_t cap,
+                               uint32_t* count);
+
+/* The focus points of the last update: hits only, in ray order.  points:
+ * HOST, cap x 3 floats; *count = the number of hits. */
+cg_status cg_shape_mesh_focii(cg_shape_mesh* sm, float* points, uint32_t cap, uint32_t* count);
 
 /* A pinhole camera: eye looking at target, `up` hint, vertical field of view
  * fov_y (radians), width x height pixels (row-major, row 0 at the top). */
