@@ -143,7 +143,8 @@ using namespace cg;
 struct cg_mesher {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;  // host-output copies overlapping placement
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     char* work = nullptr;
     size_t work_bytes = 0;
     cg_vertex* dverts = nullptr;
@@ -219,6 +220,68 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
         tm->first_ms = a;
         tm->second_ms = b;
         tm->third_ms = c;
+        tm->vertices = m->hcnt->vertices;
+        tm->faces = m->hcnt->quads;
+    }
+    return CG_OK;
+}
+
+// Device address of pinned (page-locked, mapped) host memory, else NULL.
+void* mapped_host(void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Steps 1-3 with host outputs, both pinned: the overlapped pipeline of
+// launch_mesh_to_host.  Counts and status land in m->hcnt.
+cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* shape, uint32_t res,
+                           cg_vertex* hverts_dev, uint64_t vcap, uint32_t* hidx, uint64_t icap,
+                           cg_timings* tm) {
+    CG_TRY(check_span_res(span, res));
+    CG_TRY(check_shape(shape));
+    if (m->normals == CG_NORMALS_ADJOINT && shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
+        set_error("analytic normals are built for the polar Mandelbulb (kind 2) only");
+        return CG_EINVAL;
+    }
+    const ShapeDev s = make_shape_dev(*shape);
+    const SpanSetup su = setup_span(*span, res);
+    const MeshDims d = mesh_dims(res);
+    const size_t need = mesh_workspace_layout(res, nullptr, nullptr);
+    CG_TRY(ensure(reinterpret_cast<void**>(&m->work), &m->work_bytes, need));
+    const uint64_t r3 = (uint64_t)res * res * res;
+    const uint64_t idev = icap < 18 * r3 ? icap : 18 * r3;
+    CG_TRY(ensure(reinterpret_cast<void**>(&m->didx), &m->didx_cap,
+                  (idev ? idev : 1) * sizeof(uint32_t)));
+    MeshWork w;
+    mesh_workspace_layout(res, m->work, &w);
+    cudaStream_t st = m->stream;
+    CG_CUDA(cudaEventRecord(m->ev[0], st));
+    CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
+    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
+    CG_CUDA(cudaEventRecord(m->ev[1], st));
+    CG_TRY(launch_mesh_to_host(s, su, d, w, hverts_dev, vcap, m->didx, hidx, idev, st,
+                               m->copy_stream, m->ev[2], m->ev[3], m->hcnt,
+                               m->normals == CG_NORMALS_ADJOINT));
+    CG_CUDA(cudaEventRecord(m->ev[4], st));
+    CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
+    CG_CUDA(cudaStreamSynchronize(st));
+    CG_CUDA(cudaStreamSynchronize(m->copy_stream));
+    m->last_res = res;
+    m->last_w = w;
+    if (tm) {
+        float a = 0, b = 0, c = 0, e = 0;
+        CG_CUDA(cudaEventElapsedTime(&a, m->ev[0], m->ev[1]));
+        CG_CUDA(cudaEventElapsedTime(&b, m->ev[1], m->ev[2]));
+        CG_CUDA(cudaEventElapsedTime(&c, m->ev[2], m->ev[3]));
+        CG_CUDA(cudaEventElapsedTime(&e, m->ev[3], m->ev[4]));
+        tm->first_ms = a;
+        tm->second_ms = b + e;  // cells, counts and vertex placement
+        tm->third_ms = c;       // quad indices
         tm->vertices = m->hcnt->vertices;
         tm->faces = m->hcnt->quads;
     }
@@ -317,6 +380,11 @@ cg_status cg_mesher_create(int device, cg_mesher** out) {
         return st;
     }
     for (auto& e : m->ev) cudaEventCreate(&e);
+    if ((st = cuda_status(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking),
+                          "cudaStreamCreate", __FILE__, __LINE__)) != CG_OK) {
+        cg_mesher_destroy(m);
+        return st;
+    }
     if (cudaMallocHost(reinterpret_cast<void**>(&m->hcnt), sizeof(MeshCounters)) != cudaSuccess) {
         cg_mesher_destroy(m);
         set_error("cudaMallocHost failed");
@@ -336,6 +404,7 @@ void cg_mesher_destroy(cg_mesher* m) {
     if (m->hcnt) cudaFreeHost(m->hcnt);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
+    if (m->copy_stream) cudaStreamDestroy(m->copy_stream);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;
 }
@@ -365,6 +434,17 @@ cg_status cg_generate_for_box(cg_mesher* m, const cg_span* span, const cg_shape*
     std::lock_guard<std::mutex> lk(m->mu);
     DeviceGuard g(m->device);
     CG_TRY(check_span_res(span, res));
+    // Pinned outputs: the GPU writes the vertices into them directly and the
+    // index copy overlaps the vertex placement.
+    void* vmap = vertex_cap ? mapped_host(vertices) : nullptr;
+    if (vmap && index_cap && mapped_host(indices)) {
+        CG_TRY(run_mesh_to_host(m, span, shape, res, static_cast<cg_vertex*>(vmap), vertex_cap,
+                                indices, index_cap, tm));
+        const MeshCounters c = *m->hcnt;
+        if (n_vertices) *n_vertices = c.vertices;
+        if (n_indices) *n_indices = 6ull * c.quads;
+        return finish_status(c, vertex_cap, index_cap);
+    }
     // Device staging sized to min(capacity, the largest possible count).
     const uint64_t r3 = (uint64_t)res * res * res;
     const uint64_t vdev = vertex_cap < r3 ? vertex_cap : r3;

@@ -93,6 +93,17 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
                                  bool analytic_normals = false);
 
+// The same steps for a mesh whose outputs go to host memory, reordered so
+// the transfers overlap the vertex placement: surface cells and both counts
+// first (read back: ev_counts is synchronised), then the quad indices into
+// `dev_idx` with their device-to-host copy on `copy_st`, then the vertices,
+// which k_place stores straight into `host_verts` (pinned, device-mapped).
+cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                              const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
+                              uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,
+                              cudaStream_t st, cudaStream_t copy_st, cudaEvent_t ev_counts,
+                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals);
+
 // Cell -> vertex id table of the last mesh (0xFFFFFFFF off the surface).
 cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* points,
                               cudaStream_t st);

@@ -85,18 +85,44 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
         vertex_list_row(d, r, cellbits, wordoff, rowoff[r], ~0ull, cellidx, nullptr, 0);
 }
 
-// One vertex per thread (buffer.rs:149-274).
+// One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
+// vertices and stores them through shared memory as 16-byte chunks (32
+// vertices = 896 bytes = 56 float4), so the stores are coalesced whether
+// `verts` is device memory or pinned host memory written over the C2C link.
 template <int M, bool AN>
 __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshDims d,
                                                const float* __restrict__ dists,
                                                const uint32_t* __restrict__ cellidx,
                                                MeshCounters* __restrict__ cnt,
                                                cg_vertex* __restrict__ verts, uint64_t vcap) {
+    __shared__ __align__(16) float stage[4][32 * 7];
     const uint32_t V = cnt->vertices;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool vec_ok = ((uintptr_t)verts & 15u) == 0u;
+    float* st = stage[wid];
     bool bad = false;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
-        float* o = v < vcap ? reinterpret_cast<float*>(verts + v) : nullptr;
-        bad |= !place_vertex<M, AN>(s, pp, d, dists, cellidx[v], o);
+    // warp-uniform loop over groups of 32 consecutive vertex ids
+    for (uint32_t base = blockIdx.x * blockDim.x + wid * 32; base < V;
+         base += gridDim.x * blockDim.x) {
+        const uint32_t v = base + lane;
+        float o[7] = {0, 0, 0, 0, 0, 0, 0};
+        if (v < V) bad |= !place_vertex<M, AN>(s, pp, d, dists, cellidx[v], o);
+#pragma unroll
+        for (int k = 0; k < 7; ++k) st[lane * 7 + k] = o[k];
+        __syncwarp();
+        const uint64_t room = base < vcap ? vcap - base : 0;
+        uint32_t nw = V - base < 32u ? V - base : 32u;
+        if ((uint64_t)nw > room) nw = (uint32_t)room;
+        float* dst = reinterpret_cast<float*>(verts + base);
+        if (nw == 32 && vec_ok) {
+            const float4* src4 = reinterpret_cast<const float4*>(st);
+            float4* dst4 = reinterpret_cast<float4*>(dst);
+            dst4[lane] = src4[lane];
+            if (lane < 24) dst4[32 + lane] = src4[32 + lane];
+        } else {
+            for (uint32_t i = lane; i < nw * 7; i += 32) dst[i] = st[i];
+        }
+        __syncwarp();
     }
     if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
 }
@@ -157,11 +183,41 @@ PlaceParams place_params(const SpanSetup& su) {
     return pp;
 }
 
-cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
-                                 const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                                 uint32_t* idx, uint64_t icap, cudaStream_t st,
-                                 cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals) {
+static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                              const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                              cudaStream_t st, bool analytic_normals) {
+    const PlaceParams pp = place_params(su);
+    const unsigned B = 128;
+    const unsigned G = (unsigned)sm_count() * 16;
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    case MODE_P8:
+        k_place<MODE_P8, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
+                                                 vcap);
+        break;
+    case MODE_INT:
+        k_place<MODE_INT, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
+                                                  vcap);
+        break;
+    case MODE_POLAR:
+        if (analytic_normals)
+            k_place<MODE_POLAR, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                       verts, vcap);
+        else
+            k_place<MODE_POLAR, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                        verts, vcap);
+        break;
+    default:
+        k_place<MODE_SPHERE, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                     verts, vcap);
+        break;
+    }
+    CG_CHECK_LAUNCH("k_place");
+    return CG_OK;
+}
+
+// Surface cells, their scan and the vertex list (step 2 up to placement).
+static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t st,
+                              bool signs_ready) {
     const uint32_t rows = d.res * d.res;
     CG_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(MeshCounters), st));
     if (!signs_ready) {
@@ -181,45 +237,60 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
         k_vertex_list<<<G, B, 0, st>>>(d, w.cellbits, w.wordoff, w.rowoff, w.cellidx);
         CG_CHECK_LAUNCH("k_vertex_list");
     }
-    {
-        const PlaceParams pp = place_params(su);
-        const unsigned B = 128;
-        const unsigned G = (unsigned)sm_count() * 16;
-        switch (mode_of(s, CG_NUMERICS_EXACT)) {
-        case MODE_P8:
-            k_place<MODE_P8, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
-            break;
-        case MODE_INT:
-            k_place<MODE_INT, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts, vcap);
-            break;
-        case MODE_POLAR:
-            if (analytic_normals)
-                k_place<MODE_POLAR, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx,
-                                                           w.counters, verts, vcap);
-            else
-                k_place<MODE_POLAR, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx,
-                                                            w.counters, verts, vcap);
-            break;
-        default:
-            k_place<MODE_SPHERE, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                                  vcap);
-            break;
-        }
-        CG_CHECK_LAUNCH("k_place");
-    }
-    if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
-    {
-        const unsigned B = 256, G = grid_for(rows, B, 8);
-        k_quad_count<<<G, B, 0, st>>>(w.sgn, d, w.quadcnt);
-        CG_CHECK_LAUNCH("k_quad_count");
-    }
+    return CG_OK;
+}
+
+static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStream_t st) {
+    const uint32_t rows = d.res * d.res;
+    const unsigned B = 256, G = grid_for(rows, B, 8);
+    k_quad_count<<<G, B, 0, st>>>(w.sgn, d, w.quadcnt);
+    CG_CHECK_LAUNCH("k_quad_count");
     CG_TRY(launch_exclusive_scan(w.quadcnt, w.quadoff, rows, w.scratch, &w.counters->quads, st));
-    {
-        const unsigned B = 256, G = grid_for(rows, B, 8);
-        k_quad_emit<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff,
-                                     w.quadoff, idx, icap);
-        CG_CHECK_LAUNCH("k_quad_emit");
-    }
+    return CG_OK;
+}
+
+static cg_status launch_quad_emit(const MeshDims& d, const MeshWork& w, uint32_t* idx,
+                                  uint64_t icap, cudaStream_t st) {
+    const uint32_t rows = d.res * d.res;
+    const unsigned B = 256, G = grid_for(rows, B, 8);
+    k_quad_emit<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff, w.quadoff,
+                                 idx, icap);
+    CG_CHECK_LAUNCH("k_quad_emit");
+    return CG_OK;
+}
+
+cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                                 const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                                 uint32_t* idx, uint64_t icap, cudaStream_t st,
+                                 cudaEvent_t ev_after_vertices, bool signs_ready,
+                                 bool analytic_normals) {
+    CG_TRY(launch_cells(d, w, st, signs_ready));
+    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals));
+    if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
+    CG_TRY(launch_quad_count(d, w, st));
+    CG_TRY(launch_quad_emit(d, w, idx, icap, st));
+    return CG_OK;
+}
+
+cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                              const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
+                              uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,
+                              cudaStream_t st, cudaStream_t copy_st, cudaEvent_t ev_counts,
+                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals) {
+    CG_TRY(launch_cells(d, w, st, /*signs_ready=*/true));
+    CG_TRY(launch_quad_count(d, w, st));
+    CG_CUDA(cudaMemcpyAsync(hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
+    CG_CUDA(cudaEventRecord(ev_counts, st));
+    CG_CUDA(cudaEventSynchronize(ev_counts));
+    const uint64_t ni = 6ull * hcnt->quads;
+    const uint64_t ci = ni < icap ? ni : icap;
+    CG_TRY(launch_quad_emit(d, w, dev_idx, icap, st));
+    CG_CUDA(cudaEventRecord(ev_quads, st));
+    CG_CUDA(cudaStreamWaitEvent(copy_st, ev_quads, 0));
+    if (ci)
+        CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                copy_st));
+    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, analytic_normals));
     return CG_OK;
 }
 

@@ -226,3 +226,44 @@ def test_analytic_normals(cg, orc):
     # the six-sample normal is much further from the gradient
     ang_fd = angle_deg(a[ok, 3:6], g[ok, 1:4])
     assert np.median(ang_fd) > np.median(ang)
+
+
+@pytest.mark.parametrize("res", [64, 128])
+def test_pinned_host_outputs_match_device(cg, mesher, res):
+    """Pinned host outputs take the overlapped path (vertices stored by the
+    GPU straight into host memory, the index copy overlapping placement):
+    same bits as the device-output mesh."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    vcap, icap = res ** 3 // 8, 18 * res ** 3 // 8
+    v = torch.empty((vcap, 7), dtype=torch.float32, device="cuda")
+    i = torch.empty(icap, dtype=torch.int32, device="cuda")
+    nv, ni, _ = mesher.generate_device(span, s, res, v, i)
+    vh = torch.zeros((vcap, 7), dtype=torch.float32, pin_memory=True)
+    ih = torch.zeros(icap, dtype=torch.int32, pin_memory=True)
+    vnp = vh.numpy().view(cg.VERTEX_DTYPE).reshape(-1)
+    inp = ih.numpy().view(np.uint32)
+    _, _, nv2, ni2, tm = mesher.generate(span, s, res, vertices=vnp, indices=inp)
+    assert (nv2, ni2) == (nv, ni)
+    assert np.array_equal(vh[:nv].numpy().view(np.uint32), v[:nv].cpu().numpy().view(np.uint32))
+    assert np.array_equal(ih[:ni].numpy(), i[:ni].cpu().numpy())
+    assert tm.first_ms > 0 and tm.second_ms > 0 and tm.third_ms > 0
+
+
+def test_pinned_host_outputs_capacity(cg, mesher):
+    """Too-small pinned outputs: CG_ECAPACITY with the full counts, and the
+    prefix that fits is the mesh's."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    full_v, full_i, nv, ni, _ = mesher.generate(span, s, 64)
+    vh = torch.zeros((1000, 7), dtype=torch.float32, pin_memory=True)
+    ih = torch.zeros(3000, dtype=torch.int32, pin_memory=True)
+    with pytest.raises(cg.CantucciError):
+        mesher.generate(span, s, 64, vertices=vh.numpy().view(cg.VERTEX_DTYPE).reshape(-1),
+                        indices=ih.numpy().view(np.uint32))
+    got = vh.numpy().view(np.uint32)
+    want = full_v[:1000].view(np.float32).reshape(-1, 7).view(np.uint32)
+    assert np.array_equal(got, want)
+    assert np.array_equal(ih.numpy().view(np.uint32), full_i[:3000])
