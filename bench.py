@@ -460,6 +460,7 @@ def run_ours(args, rank, world, local_rank):
     shape = cg.Mandelbulb(**SHAPE)
     span = cg.Span(*W.SPAN_C1)
     res = args.res
+    _ffi.check(lib.cg_set_option(b"de_grid_kernel", args.de_kernel))
     n_pts = (res + 1) ** 3
     mesher = cg.Mesher(dev)
     sp = C.c_void_p()
@@ -547,7 +548,10 @@ def run_ours(args, rank, world, local_rank):
     _ffi.check(lib.cg_fp32_peak_probe(20000, 1, C.byref(peak2)))
     peak_tf = peak.value / 1e12
     roofline = {
-        "bound": "fp32", "kernel": "k_de_grid", "achieved": achieved, "peak": peak_tf,
+        "bound": "fp32",
+        "kernel": {0: "k_de_grid_brick", 1: "k_de_grid", 2: "k_de_grid_brick",
+                   3: "k_de_grid_p8x2"}[args.de_kernel],
+        "achieved": achieved, "peak": peak_tf,
         "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
         "peak_source": "measured in this run: FFMA chains, 2 flop per FFMA (FP32 pipe peak; "
                        "not in MEASURED_PEAKS.json)",
@@ -563,7 +567,7 @@ def run_ours(args, rank, world, local_rank):
     if args.traffic is not None:
         roofline["traffic"] = args.traffic
         roofline["traffic_source"] = "--traffic (DRAM bytes per launch from an ncu capture)"
-    elif res == RES:
+    elif res == RES and args.de_kernel in (0, 2):
         roofline["traffic"] = DE_TRAFFIC_RES512
         roofline["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one "
                                       "k_de_grid_brick launch at res 512 (ncu --set full, "
@@ -620,6 +624,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="step-1 kernel: 0 auto (2x4x4 bricks), 1 linear, 2 bricks, 3 packed "
+                         "f32x2 (all bit-identical)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, normals and depth-map measurements")
     ap.add_argument("--traffic", type=float, default=None,
