@@ -111,17 +111,16 @@ __device__ __forceinline__ void rotate_p8(float x, float y, float z, float& ox, 
     oz = O::mul(O::mul(O::mul(O::mul(8.0f, z), O::sqrt(rxy2)), O::sub(z2, rxy2)), Z);
 }
 
-// rotate_on_z_axis (mandelbulb.rs:114-126).
+// rotate_on_z_axis (mandelbulb.rs:114-126): x' = y' = 0, and z' as returned.
+// Out of line (the path is rare) and with no reference parameters, so the
+// call needs no stack slots in the hot loop.
 template <class O>
-__device__ __noinline__ void rotate_axis(int32_t P, float x, float y, float z, float& ox,
-                                         float& oy, float& oz) {
+__device__ __noinline__ float rotate_axis_z(int32_t P, float x, float y, float z) {
     const float old_radius = magnitude<O>(x, y, z);
     float theta = acosf(O::div(z, old_radius));
     const float new_radius = powi<O>(old_radius, P);
     theta = O::mul(theta, (float)P);
-    ox = 0.0f;
-    oy = 0.0f;
-    oz = O::mul(new_radius, cosf(theta));
+    return O::mul(new_radius, cosf(theta));
 }
 
 // rotate_inner_px_generic (mandelbulb.rs:128-146).
@@ -168,7 +167,9 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
         dr = O::add(O::mul(O::mul(powi<O>(r, P - 1), Pf), dr), 1.0f);
         float nx, ny, nz;
         if (on_z_axis(zx, zy)) {
-            rotate_axis<O>(P, zx, zy, zz, nx, ny, nz);
+            nx = 0.0f;
+            ny = 0.0f;
+            nz = rotate_axis_z<O>(P, zx, zy, zz);
         } else if (P8) {
             rotate_p8<O>(zx, zy, zz, nx, ny, nz);
         } else {
@@ -336,17 +337,15 @@ __device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailo
             O::up(nx, oxA, oxB);
             O::up(ny, oyA, oyB);
             O::up(nz, ozA, ozB);
-            if (aA && on_z_axis(xA, yA)) {
-                rotate_axis<Exact>(8, xA, yA, zA, oxA, oyA, ozA);
-                oxA = -oxA;
-                oyA = -oyA;
-                ozA = -ozA;
+            if (aA && on_z_axis(xA, yA)) {  // negated outputs: -(0), -(0), -z'
+                oxA = -0.0f;
+                oyA = -0.0f;
+                ozA = -rotate_axis_z<Exact>(8, xA, yA, zA);
             }
             if (aB && on_z_axis(xB, yB)) {
-                rotate_axis<Exact>(8, xB, yB, zB, oxB, oyB, ozB);
-                oxB = -oxB;
-                oyB = -oyB;
-                ozB = -ozB;
+                oxB = -0.0f;
+                oyB = -0.0f;
+                ozB = -rotate_axis_z<Exact>(8, xB, yB, zB);
             }
             nx = O::pk(oxA, oxB);
             ny = O::pk(oyA, oyB);
