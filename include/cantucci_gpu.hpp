@@ -8,6 +8,8 @@
 //   Span, create_spans     src/octree/mod.rs:13-32,315-329
 //   MeshBuffer, Timings    src/mesh/buffer.rs:24-42,395-433
 //   Vertex                 src/mesh/mod.rs:255-261 (== cg_vertex)
+//   Camera, Projection     src/camera.rs:14-190 (the fields the mesher needs)
+//   ShapeMesh              src/mesh/mod.rs:24-243 (update; leaves instead of draw)
 // Where the reference panics (assert!, lerp outside [0,1]) these throw
 // cantucci::Panic.  Link with -lcantucci_gpu -lcudart.
 #pragma once
@@ -217,6 +219,80 @@ struct MeshBuffer {
         b.indices.resize(ni);
         return {std::move(b), Timings{t.first_ms, t.second_ms, t.third_ms, t.vertices, t.faces}};
     }
+};
+
+// Camera + Projection: position, look direction (normalised by the library),
+// vertical field of view in radians, aspect ratio, near and far plane.
+struct Camera {
+    Point3 position{0.0f, -2.5f, 0.0f};
+    Point3 direction{0.0f, 1.0f, 0.0f};
+    float fov = 1.0471976f;  // 60 degrees
+    float aspect_ratio = 1.0f;
+    float near_plane = 0.01f, far_plane = 100.0f;
+
+    cg_view to_c() const {
+        cg_view v{};
+        v.position[0] = position.x;
+        v.position[1] = position.y;
+        v.position[2] = position.z;
+        v.direction[0] = direction.x;
+        v.direction[1] = direction.y;
+        v.direction[2] = direction.z;
+        v.fov_y = fov;
+        v.aspect = aspect_ratio;
+        v.near_plane = near_plane;
+        v.far_plane = far_plane;
+        return v;
+    }
+};
+
+// ShapeMesh: the octree of meshed leaves, refined around the camera's focus
+// points; all jobs of an update are one batched GPU run.
+class ShapeMesh {
+public:
+    struct Leaf {
+        Span span;
+        uint32_t status;  // 0 empty, 1 requested, 2 ready
+        uint32_t depth;
+        const Vertex* vertices;  // device memory, valid until the next update
+        const uint32_t* indices;
+        uint32_t n_vertices, n_indices;
+    };
+
+    explicit ShapeMesh(const Shape& shape, uint32_t resolution = 64, int device = 0) {
+        const cg_shape s = shape.to_cg_shape();
+        const cg_span b = shape.bounding_box().to_c();
+        check(cg_shape_mesh_create(device, &s, &b, resolution, &sm_));
+    }
+    ~ShapeMesh() { cg_shape_mesh_destroy(sm_); }
+    ShapeMesh(const ShapeMesh&) = delete;
+    ShapeMesh& operator=(const ShapeMesh&) = delete;
+
+    // ShapeMesh::update; wait = block for the jobs started by earlier updates.
+    cg_lod_stats update(const Camera& camera, bool wait = false) {
+        const cg_view v = camera.to_c();
+        cg_lod_stats st{};
+        check(cg_shape_mesh_update(sm_, &v, wait ? 1u : 0u, &st));
+        return st;
+    }
+
+    // The leaves in Octree::iter order.
+    std::vector<Leaf> leaves() const {
+        uint32_t n = 0;
+        check(cg_shape_mesh_leaves(sm_, nullptr, 0, &n));
+        std::vector<cg_leaf> raw(n);
+        check(cg_shape_mesh_leaves(sm_, raw.data(), n, &n));
+        std::vector<Leaf> out;
+        out.reserve(n);
+        for (const cg_leaf& l : raw)
+            out.push_back({{{l.span.start[0], l.span.start[1], l.span.start[2]},
+                            {l.span.end[0], l.span.end[1], l.span.end[2]}},
+                           l.status, l.depth, l.vertices, l.indices, l.n_vertices, l.n_indices});
+        return out;
+    }
+
+private:
+    cg_shape_mesh* sm_ = nullptr;
 };
 
 }  // namespace cantucci

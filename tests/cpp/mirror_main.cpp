@@ -41,9 +41,26 @@ int main(int argc, char** argv) {
         panicked = p.status == CG_EINVAL;
     }
     const auto children = create_spans(span);
+
+    // ShapeMesh: two updates from afar mesh the 64 initial leaves; a camera
+    // near the surface then splits some of them.
+    ShapeMesh lod(shape, 32);
+    Camera far_cam;
+    far_cam.position = {0.0f, -30.0f, 0.0f};
+    lod.update(far_cam, true);
+    const cg_lod_stats s2 = lod.update(far_cam, true);
+    Camera near_cam;
+    near_cam.position = {0.05f, -1.45f, 0.1f};
+    near_cam.direction = {0.0f, 1.0f, 0.05f};
+    const cg_lod_stats s3 = lod.update(near_cam, true);
+    size_t ready = 0;
+    for (const auto& l : lod.leaves()) ready += l.status == 2;
+
     FILE* f = fopen((out + "/summary.txt").c_str(), "w");
-    fprintf(f, "%zu %zu %u %u %d %.7g %d\n", buf.vertices.size(), buf.indices.size(), t.vertices,
-            t.faces, panicked, children[3].start.y, (int)Sphere({0, 0, 0}, 1.0f).contains({0.5f, 0, 0}));
+    fprintf(f, "%zu %zu %u %u %d %.7g %d %u %u %u %zu\n", buf.vertices.size(), buf.indices.size(),
+            t.vertices, t.faces, panicked, children[3].start.y,
+            (int)Sphere({0, 0, 0}, 1.0f).contains({0.5f, 0, 0}), s2.collected, s3.splits,
+            s3.leaves, ready);
     fclose(f);
     return 0;
 }

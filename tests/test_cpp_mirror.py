@@ -42,7 +42,10 @@ def test_cpp_mirror_compiles(mirror_bin):
 def test_cpp_mirror_meshes_like_reference(mirror_bin, golden, tmp_path):
     r = subprocess.run([mirror_bin, str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
-    nv, ni, tv, tf, panicked, child3_y, sphere_in = open(tmp_path / "summary.txt").read().split()
+    (nv, ni, tv, tf, panicked, child3_y, sphere_in, collected, splits, leaves,
+     ready) = open(tmp_path / "summary.txt").read().split()
+    assert int(collected) == 64 and int(splits) > 0
+    assert int(leaves) == 64 + 7 * int(splits) and int(ready) == 64 - int(splits)
     assert [int(nv), int(ni)] == golden["c1_counts"].tolist()
     assert int(tf) * 6 == int(ni) and int(tv) == int(nv)
     idx = np.fromfile(tmp_path / "indices.u32", np.uint32)
