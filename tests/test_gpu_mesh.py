@@ -267,3 +267,41 @@ def test_pinned_host_outputs_capacity(cg, mesher):
     want = full_v[:1000].view(np.float32).reshape(-1, 7).view(np.uint32)
     assert np.array_equal(got, want)
     assert np.array_equal(ih.numpy().view(np.uint32), full_i[:3000])
+
+
+@pytest.mark.parametrize("span,res", [
+    (([1.5, 1.5, 1.5], [2.0, 2.0, 2.0]), 16),      # all outside: no surface
+    (([-0.05, -0.05, -0.05], [0.05, 0.05, 0.05]), 8),  # all inside (the origin is NaN, "inside")
+    (([-1.2, -1.2, -1.2], [1.2, 1.2, 1.2]), 2),     # the smallest resolution
+    (([-0.9, 0.1, -0.3], [-0.5, 0.5, 0.1]), 4),
+])
+def test_edge_spans_match_oracle(cg, orc, mesher, span, res):
+    """Includes res 2 over the whole box, whose widened grid has the origin
+    (NaN) next to outside corners: the reference panics there, and both
+    sides report CG_ELERP with the same completed mesh."""
+    s = cg.Mandelbulb(8, 15, 2.5)
+    v, i, nv, ni, _ = mesher.generate(cg.Span(*span), s, res, strict=False)
+    ref = orc.generate_for_box(orc.mandelbulb(8, 15, 2.5),
+                               np.array(span, np.float32).ravel(), res)
+    assert mesher.last_status == ref["rc"]
+    assert np.array_equal(i[:ni], ref["indices"])
+    assert nv == len(ref["vertices"])
+    if nv:
+        np.testing.assert_allclose(as7(v[:nv])[:, :3], as7(ref["vertices"])[:, :3],
+                                   rtol=0, atol=1e-6)
+
+
+def test_empty_mesh_batch_and_device(cg, mesher):
+    """A span with no surface gives zero counts on every path."""
+    import torch
+    from cantucci_gb300.batch import BatchMesher
+    s = cg.Mandelbulb(8, 15, 2.5)
+    sp = cg.Span([1.5, 1.5, 1.5], [2.0, 2.0, 2.0])
+    v = torch.empty((16, 7), dtype=torch.float32, device="cuda")
+    i = torch.empty(16, dtype=torch.int32, device="cuda")
+    assert mesher.generate_device(sp, s, 32, v, i)[:2] == (0, 0)
+    b = BatchMesher(np.array([[1.5, 1.5, 1.5, 2.0, 2.0, 2.0]], np.float32), [32])
+    out = b.run(s, graph=True)
+    vv, ii = out.mesh(0)
+    assert len(vv) == 0 and len(ii) == 0 and out.status == 0
+    b.close()
