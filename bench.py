@@ -358,10 +358,11 @@ def extra_depth_fit(dev, steps=300):
 
 def extra_de_variants(dev, res=RES):
     """The step-1 DE alone (cg_de_span_grid, no sign words) on the 513^3
-    span in three numerics: the exact P=8 polynomial (bit-faithful), the
+    span in several numerics: the exact P=8 polynomial (bit-faithful), the
     same polynomial FMA-contracted with approximate division and square root
-    (not bit-faithful), and the real-power polar form at power 8.0 (the
-    reference's GLSL estimator, transcendental-bound).  Flop rates use the
+    (not bit-faithful), the real-power polar form at power 8.0 (the
+    reference's GLSL estimator, transcendental-bound), and P=6 through the
+    reference's trig path and through the trig-free complex-power form.  Flop rates use the
     exact path's algorithmic count (76 per iteration, the exact path's
     iteration totals) for both P=8 variants."""
     import torch
@@ -380,11 +381,13 @@ def extra_de_variants(dev, res=RES):
     _ffi.check(lib.cg_fp32_peak_probe(20000, 0, C.byref(peak)))
     res_out = {"workload": "%d^3 corners of [-1.2,1.2]^3 widened, max_iters 15" % n,
                "fp32_peak_tflops": peak.value / 1e12}
+    p6 = cg.Mandelbulb(6, 15, 2.5)
     for name, shape in (("exact_p8", exact), ("fast_p8", exact.fast()),
-                        ("polar_p8.0", cg.MandelbulbPolar(8.0, 15, 2.5))):
+                        ("polar_p8.0", cg.MandelbulbPolar(8.0, 15, 2.5)),
+                        ("trig_p6", p6), ("trig_free_p6", p6.fast())):
         ms = _time_cuda(lambda: shape.span_grid(span, res, out=out), reps=5, warm=2)
         e = {"ms": ms, "pts_per_s": n ** 3 / (ms * 1e-3)}
-        if name != "polar_p8.0":
+        if name in ("exact_p8", "fast_p8"):
             e["tflops"] = flops / (ms * 1e-3) / 1e12
             e["frac_of_fp32_peak"] = e["tflops"] * 1e12 / peak.value
         res_out[name] = e

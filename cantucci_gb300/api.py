@@ -157,7 +157,9 @@ class Mandelbulb(Shape):
         return Span([-1.2, -1.2, -1.2], [1.2, 1.2, 1.2])
 
     def fast(self) -> "Mandelbulb":
-        """Same shape with FMA-contracted numerics (not bit-faithful)."""
+        """Same shape with fast numerics (not bit-faithful): P=8 FMA-contracted
+        with approximate division and square root, other integer powers
+        through the trig-free complex-power form."""
         m = Mandelbulb(self.power, self.max_iters, self.bailout)
         m.numerics = _ffi.CG_NUMERICS_FAST
         return m

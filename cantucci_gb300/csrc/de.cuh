@@ -46,6 +46,15 @@ struct Exact {
     static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
 };
 
+// Plain float operations (the compiler may contract them).
+struct Fast {
+    static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+    static __device__ __forceinline__ float add(float a, float b) { return a + b; }
+    static __device__ __forceinline__ float sub(float a, float b) { return a - b; }
+    static __device__ __forceinline__ float div(float a, float b) { return a / b; }
+    static __device__ __forceinline__ float sqrt(float a) { return sqrtf(a); }
+};
+
 // Vec3::magnitude with SSE4.1 (mandelbulb.rs:412-418): dpps sums the lane
 // products as (x*x + y*y) + z*z.
 template <class O>
@@ -443,8 +452,78 @@ __device__ __forceinline__ float mandelbulb_p8_fast(uint32_t max_iters, float ba
     return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
 }
 
+// Integer power P >= 1 of the complex number (re, im), square-and-multiply.
+__device__ __forceinline__ void cpow_int(float re, float im, int32_t P, float& ore, float& oim) {
+    float rr = 1.0f, ri = 0.0f, br = re, bi = im;
+    uint32_t m = (uint32_t)P;
+    while (m) {
+        if (m & 1u) {
+            const float t = fmaf(rr, br, -ri * bi);
+            ri = fmaf(rr, bi, ri * br);
+            rr = t;
+        }
+        m >>= 1;
+        if (m) {
+            const float t = fmaf(br, br, -bi * bi);
+            bi = 2.0f * br * bi;
+            br = t;
+        }
+    }
+    ore = rr;
+    oim = ri;
+}
+
+// Trig-free form of rotate_inner_px_generic (mandelbulb.rs:128-146) for an
+// integer power P (CG_NUMERICS_FAST): with theta = acos(z / r) and
+// phi = atan2(y, x), the unit complex numbers a = (z + i rho) / r and
+// b = (x + i y) / rho (rho = |(x, y)|) have arguments theta and phi, so
+//   cos(P theta) + i sin(P theta) = a^P,   cos(P phi) + i sin(P phi) = b^P,
+// and x' = r^P Im(a^P) Re(b^P), y' = r^P Im(a^P) Im(b^P), z' = r^P Re(a^P):
+// two square-and-multiply complex powers instead of acos, atan2 and two
+// sincos.  On the z axis (x = y = 0, rotate_on_z_axis) b is undefined and
+// x' = y' = 0, z' = r^P Re(a^P) as before.  Not bit-faithful to the
+// reference's libm path (which is not bit-reproducible itself).
+__device__ __forceinline__ float mandelbulb_int_poly(int32_t P, uint32_t max_iters, float bailout,
+                                                     float px, float py, float pz) {
+    float zx = px, zy = py, zz = pz, dr = 1.0f, r = 0.0f;
+    const float Pf = (float)P;
+    for (uint32_t i = 0; i < max_iters; ++i) {
+        const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+        r = sqrtf(r2);
+        if (r > bailout) break;
+        const float rp1 = powi<Fast>(r, P - 1);
+        dr = fmaf(rp1 * Pf, dr, 1.0f);
+        const float rho2 = fmaf(zx, zx, zy * zy);
+        const float rho = sqrtf(rho2);
+        const float inv_r = 1.0f / r;
+        float ar, ai;
+        cpow_int(zz * inv_r, rho * inv_r, P, ar, ai);
+        const float rP = rp1 * r;
+        float nx = 0.0f, ny = 0.0f;
+        if (rho > 0.0f) {
+            const float inv_rho = 1.0f / rho;
+            float br, bi;
+            cpow_int(zx * inv_rho, zy * inv_rho, P, br, bi);
+            const float k = rP * ai;
+            nx = k * br;
+            ny = k * bi;
+        }
+        zx = nx + px;
+        zy = ny + py;
+        zz = fmaf(rP, ar, pz);
+    }
+    return x86_nan(0.5f * logf(r) * r / dr);
+}
+
 // Kernel modes.
-enum Mode { MODE_P8 = 0, MODE_INT = 1, MODE_POLAR = 2, MODE_SPHERE = 3, MODE_P8_FAST = 4 };
+enum Mode {
+    MODE_P8 = 0,
+    MODE_INT = 1,
+    MODE_POLAR = 2,
+    MODE_SPHERE = 3,
+    MODE_P8_FAST = 4,
+    MODE_INT_POLY = 5
+};
 
 template <int M>
 __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
@@ -452,6 +531,7 @@ __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float
     if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
     if (M == MODE_POLAR) return polar_de(s, x, y, z);
     if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
+    if (M == MODE_INT_POLY) return mandelbulb_int_poly(s.power, s.max_iters, s.bailout, x, y, z);
     return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
 }
 
@@ -461,7 +541,7 @@ __host__ __device__ __forceinline__ int mode_of(const ShapeDev& s, uint32_t nume
     if (s.kind == CG_SHAPE_SPHERE) return MODE_SPHERE;
     if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return MODE_POLAR;
     if (s.power == 8) return numerics == CG_NUMERICS_FAST ? MODE_P8_FAST : MODE_P8;
-    return MODE_INT;
+    return numerics == CG_NUMERICS_FAST && s.power >= 1 ? MODE_INT_POLY : MODE_INT;
 }
 
 }  // namespace cg

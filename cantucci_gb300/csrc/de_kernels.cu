@@ -213,6 +213,7 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
     case MODE_INT: k_de_points<MODE_INT><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_POLAR: k_de_points<MODE_POLAR><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_SPHERE: k_de_points<MODE_SPHERE><<<G, B, 0, st>>>(s, pts, n, out); break;
+    case MODE_INT_POLY: k_de_points<MODE_INT_POLY><<<G, B, 0, st>>>(s, pts, n, out); break;
     default: k_de_points<MODE_P8_FAST><<<G, B, 0, st>>>(s, pts, n, out); break;
     }
     CG_CHECK_LAUNCH("k_de_points");
@@ -298,6 +299,7 @@ cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32
     case MODE_INT: launch_grid_mode<MODE_INT>(s, g, out, sgn, W, st); break;
     case MODE_POLAR: launch_grid_mode<MODE_POLAR>(s, g, out, sgn, W, st); break;
     case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st); break;
+    case MODE_INT_POLY: launch_grid_mode<MODE_INT_POLY>(s, g, out, sgn, W, st); break;
     default: launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st); break;
     }
     CG_CHECK_LAUNCH("k_de_grid");

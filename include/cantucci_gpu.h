@@ -49,7 +49,9 @@ enum {
 /* Numerics of the distance estimator. */
 enum {
     CG_NUMERICS_EXACT = 0,  /* IEEE f32, reference operation order: bit-identical loop state */
-    CG_NUMERICS_FAST = 1    /* FMA-contracted, approximate div/sqrt; not bit-faithful */
+    CG_NUMERICS_FAST = 1    /* not bit-faithful: P=8 FMA-contracted with approximate div/sqrt;
+                               other integer powers trig-free (complex powers, no acos/atan2/
+                               sin/cos) */
 };
 
 /* Normals of the mesher. */

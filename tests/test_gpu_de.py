@@ -214,3 +214,22 @@ def test_invalid_shape_raises(cg):
         m = cg.Mandelbulb(8, 15, 2.5)
         m.max_iters = 0
         m.batch_min_distance_from(np.zeros((4, 3), np.float32))
+
+
+@pytest.mark.parametrize("P", [3, 6, 10])
+def test_int_power_trig_free_path(cg, orc, P):
+    """Fast numerics for integer P != 8: the complex-power form is as close
+    to the FP64 trig formula as the (libm) trig path is."""
+    import torch
+    pts = W.uniform_points(200_000, seed=30 + P)
+    p = torch.as_tensor(pts).cuda()
+    exact = cg.Mandelbulb(P, 15, 2.5)
+    d_exact = exact.batch_min_distance_from(p).cpu().numpy().astype(np.float64)
+    d_fast = exact.fast().batch_min_distance_from(p).cpu().numpy().astype(np.float64)
+    ref = orc.de_f64(orc.mandelbulb(P, 15, 2.5), pts)
+    ok = np.isfinite(ref)
+    scale = np.maximum(np.abs(ref[ok]), 1e-6)
+    close_fast = np.mean(np.abs(d_fast[ok] - ref[ok]) / scale < 1e-3)
+    close_exact = np.mean(np.abs(d_exact[ok] - ref[ok]) / scale < 1e-3)
+    assert close_fast >= 0.99 and close_fast >= close_exact - 0.005, (close_fast, close_exact)
+    assert np.mean(np.sign(d_fast[ok]) == np.sign(ref[ok])) >= 0.999
