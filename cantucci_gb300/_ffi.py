@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "CG_OK", 1: "CG_EINVAL", 2: "CG_ECAPACITY", 3: "CG_ELERP", 4:
 CG_SHAPE_MANDELBULB, CG_SHAPE_SPHERE, CG_SHAPE_MANDELBULB_POLAR = 0, 1, 2
 CG_NUMERICS_EXACT, CG_NUMERICS_FAST = 0, 1
 CG_NORMALS_FD, CG_NORMALS_ADJOINT = 0, 1
+CG_CROSSINGS_LERP, CG_CROSSINGS_ROOT = 0, 1
 
 
 class CgShape(C.Structure):
@@ -101,6 +102,7 @@ SIGNATURES = [
     ("cg_mesher_create", _i32, [_i32, C.POINTER(_vp)]),
     ("cg_mesher_destroy", None, [_vp]),
     ("cg_mesher_set_normals", _i32, [_vp, _u32]),
+    ("cg_mesher_set_crossings", _i32, [_vp, _u32, _u32]),
     ("cg_generate_for_box", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
                                    C.POINTER(_u64), C.POINTER(_u64), _tmp]),
     ("cg_generate_for_box_device", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,

@@ -272,6 +272,13 @@ class Mesher:
         modes = {"fd": _ffi.CG_NORMALS_FD, "analytic": _ffi.CG_NORMALS_ADJOINT}
         check(self._lib.cg_mesher_set_normals(self.handle, modes[mode]))
 
+    def set_crossings(self, mode: str, iters: int = 4):
+        """"lerp": the reference's distance-weighted corner lerp (default);
+        "root": each crossing at the DE's root along its edge, `iters`
+        regula falsi steps (same cells and indices, vertices on the surface)."""
+        modes = {"lerp": _ffi.CG_CROSSINGS_LERP, "root": _ffi.CG_CROSSINGS_ROOT}
+        check(self._lib.cg_mesher_set_crossings(self.handle, modes[mode], int(iters)))
+
     def generate(self, span: Span, shape: Shape, resolution: int, vertex_cap=None,
                  index_cap=None, vertices=None, indices=None, strict: bool = True):
         """Mesh into host numpy arrays (pinned torch tensors also accepted).

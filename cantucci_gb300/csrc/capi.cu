@@ -153,6 +153,7 @@ struct cg_mesher {
     size_t didx_cap = 0;
     MeshCounters* hcnt = nullptr;  // pinned
     uint32_t normals = CG_NORMALS_FD;
+    uint32_t root_iters = 0;  // CG_CROSSINGS_LERP
     uint32_t last_res = 0;
     MeshWork last_w{};
     std::mutex mu;
@@ -206,7 +207,8 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
                                   /*signs_ready=*/true,
-                                  /*analytic_normals=*/m->normals == CG_NORMALS_ADJOINT));
+                                  /*analytic_normals=*/m->normals == CG_NORMALS_ADJOINT,
+                                  m->root_iters));
     CG_CUDA(cudaEventRecord(m->ev[3], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -266,7 +268,7 @@ cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* sh
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     CG_TRY(launch_mesh_to_host(s, su, d, w, hverts_dev, vcap, m->didx, hidx, idev, st,
                                m->copy_stream, m->ev[2], m->ev[3], m->hcnt,
-                               m->normals == CG_NORMALS_ADJOINT));
+                               m->normals == CG_NORMALS_ADJOINT, m->root_iters));
     CG_CUDA(cudaEventRecord(m->ev[4], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -416,6 +418,17 @@ cg_status cg_mesher_set_normals(cg_mesher* m, uint32_t normals) {
     }
     std::lock_guard<std::mutex> lk(m->mu);
     m->normals = normals;
+    return CG_OK;
+}
+
+cg_status cg_mesher_set_crossings(cg_mesher* m, uint32_t crossings, uint32_t iters) {
+    if (!m || crossings > CG_CROSSINGS_ROOT ||
+        (crossings == CG_CROSSINGS_ROOT && (iters < 1 || iters > 16))) {
+        set_error("crossings: CG_CROSSINGS_LERP, or CG_CROSSINGS_ROOT with 1..16 iterations");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(m->mu);
+    m->root_iters = crossings == CG_CROSSINGS_ROOT ? iters : 0;
     return CG_OK;
 }
 

@@ -89,12 +89,13 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
 // vertices and stores them through shared memory as 16-byte chunks (32
 // vertices = 896 bytes = 56 float4), so the stores are coalesced whether
 // `verts` is device memory or pinned host memory written over the C2C link.
-template <int M, bool AN>
+template <int M, bool AN, bool ROOT>
 __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshDims d,
                                                const float* __restrict__ dists,
                                                const uint32_t* __restrict__ cellidx,
                                                MeshCounters* __restrict__ cnt,
-                                               cg_vertex* __restrict__ verts, uint64_t vcap) {
+                                               cg_vertex* __restrict__ verts, uint64_t vcap,
+                                               uint32_t root_iters) {
     __shared__ __align__(16) float stage[4][32 * 7];
     const uint32_t V = cnt->vertices;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -106,7 +107,7 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
          base += gridDim.x * blockDim.x) {
         const uint32_t v = base + lane;
         float o[7] = {0, 0, 0, 0, 0, 0, 0};
-        if (v < V) bad |= !place_vertex<M, AN>(s, pp, d, dists, cellidx[v], o);
+        if (v < V) bad |= !place_vertex<M, AN, ROOT>(s, pp, d, dists, cellidx[v], o, root_iters);
 #pragma unroll
         for (int k = 0; k < 7; ++k) st[lane * 7 + k] = o[k];
         __syncwarp();
@@ -183,32 +184,39 @@ PlaceParams place_params(const SpanSetup& su) {
     return pp;
 }
 
-static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+template <int M, bool AN>
+static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                              cudaStream_t st, bool analytic_normals) {
-    const PlaceParams pp = place_params(su);
+                              cudaStream_t st, uint32_t root_iters) {
     const unsigned B = 128;
     const unsigned G = (unsigned)sm_count() * 16;
+    if (root_iters)
+        k_place<M, AN, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
+                                              vcap, root_iters);
+    else
+        k_place<M, AN, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
+                                               vcap, 0);
+}
+
+static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                              const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                              cudaStream_t st, bool analytic_normals, uint32_t root_iters) {
+    const PlaceParams pp = place_params(su);
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
     case MODE_P8:
-        k_place<MODE_P8, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                                 vcap);
+        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, root_iters);
         break;
     case MODE_INT:
-        k_place<MODE_INT, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                                  vcap);
+        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, root_iters);
         break;
     case MODE_POLAR:
         if (analytic_normals)
-            k_place<MODE_POLAR, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                       verts, vcap);
+            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, root_iters);
         else
-            k_place<MODE_POLAR, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                        verts, vcap);
+            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, root_iters);
         break;
     default:
-        k_place<MODE_SPHERE, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                     verts, vcap);
+        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, root_iters);
         break;
     }
     CG_CHECK_LAUNCH("k_place");
@@ -263,9 +271,9 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals) {
+                                 bool analytic_normals, uint32_t root_iters) {
     CG_TRY(launch_cells(d, w, st, signs_ready));
-    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals));
+    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals, root_iters));
     if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
     CG_TRY(launch_quad_count(d, w, st));
     CG_TRY(launch_quad_emit(d, w, idx, icap, st));
@@ -276,7 +284,8 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
                               const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
                               uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,
                               cudaStream_t st, cudaStream_t copy_st, cudaEvent_t ev_counts,
-                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals) {
+                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals,
+                              uint32_t root_iters) {
     CG_TRY(launch_cells(d, w, st, /*signs_ready=*/true));
     CG_TRY(launch_quad_count(d, w, st));
     CG_CUDA(cudaMemcpyAsync(hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
@@ -290,7 +299,7 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     if (ci)
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 copy_st));
-    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, analytic_normals));
+    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, analytic_normals, root_iters));
     return CG_OK;
 }
 

@@ -87,16 +87,33 @@ struct PlaceParams {
 
 PlaceParams place_params(const SpanSetup& su);
 
+// Corner k of a cell's eight distances without a dynamic register index.
+__device__ __forceinline__ float pick8(const float (&dd)[8], uint32_t k) {
+    float v = dd[0];
+#pragma unroll
+    for (uint32_t j = 1; j < 8; ++j) v = k == j ? dd[j] : v;
+    return v;
+}
+
+// EDGES (buffer.rs:155-176) packed 4 bits per edge: from / to corner of edge k.
+constexpr uint64_t kEdgeFrom = 0x642054103210ull;  // 0,1,2,3, 0,1,4,5, 0,2,4,6
+constexpr uint64_t kEdgeTo = 0x753176327654ull;    // 4,5,6,7, 2,3,6,7, 1,3,5,7
+
 // Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
 // crossings, DE at the vertex and the six-sample central-difference normal.
 // With AN (polar form only) the normal is instead the normalised analytic
 // gradient from one forward-mode pass, which also gives the DE at the vertex
-// (the same bits as the estimator's).
+// (the same bits as the estimator's).  With ROOT each crossing is not the
+// reference's distance-weighted lerp but the root of the DE along the edge,
+// found by root_iters Illinois (regula falsi) steps from the edge's corner
+// distances -- the refinement buffer.rs:178-186 leaves for
+// later (issue #1); the cell table and the index list do not change.
 // Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
-template <int M, bool AN = false>
+template <int M, bool AN = false, bool ROOT = false>
 __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
                                              const MeshDims& d, const float* __restrict__ dists,
-                                             uint32_t c, float* __restrict__ o) {
+                                             uint32_t c, float* __restrict__ o,
+                                             uint32_t root_iters = 0) {
     const uint32_t z = c % d.res, xy = c / d.res, y = xy % d.res, x = xy / d.res;
     float dd[8];
 #pragma unroll
@@ -111,13 +128,14 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
     const uint8_t EF[12] = {0, 1, 2, 3, 0, 1, 4, 5, 0, 2, 4, 6};
     const uint8_t ET[12] = {4, 5, 6, 7, 2, 3, 6, 7, 1, 3, 5, 7};
     float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    uint32_t count = 0;
+    uint32_t count = 0, xmask = 0;
     bool bad = false;
 #pragma unroll
     for (int k = 0; k < 12; ++k) {
         const int from = EF[k], to = ET[k];
         const float df0 = dd[from], dt0 = dd[to];
         if ((__float_as_uint(df0) >> 31) == (__float_as_uint(dt0) >> 31)) continue;
+        xmask |= 1u << k;
         float df, dt;
         if (df0 < 0.0f) {
             df = df0;
@@ -150,6 +168,45 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
         sy = __fadd_rn(sy, __fadd_rn(__fmul_rn(ay, omt), __fmul_rn(by, wgt)));
         sz = __fadd_rn(sz, __fadd_rn(__fmul_rn(az, omt), __fmul_rn(bz, wgt)));
         ++count;
+    }
+    if constexpr (ROOT) {
+        sx = sy = sz = 0.0f;
+#pragma unroll 1
+        for (uint32_t m = xmask; m; m &= m - 1) {
+            const uint32_t k = __ffs(m) - 1;
+            const uint32_t from = (uint32_t)(kEdgeFrom >> (4 * k)) & 7u;
+            const uint32_t to = (uint32_t)(kEdgeTo >> (4 * k)) & 7u;
+            const float ax = p0x + (((from >> 2) & 1) ? pp.step[0] : 0.0f);
+            const float ay = p0y + (((from >> 1) & 1) ? pp.step[1] : 0.0f);
+            const float az = p0z + ((from & 1) ? pp.step[2] : 0.0f);
+            const float ex = (((to >> 2) & 1) ? pp.step[0] : 0.0f) - (((from >> 2) & 1) ? pp.step[0] : 0.0f);
+            const float ey = (((to >> 1) & 1) ? pp.step[1] : 0.0f) - (((from >> 1) & 1) ? pp.step[1] : 0.0f);
+            const float ez = ((to & 1) ? pp.step[2] : 0.0f) - ((from & 1) ? pp.step[2] : 0.0f);
+            float f0 = pick8(dd, from), f1 = pick8(dd, to);
+            const uint32_t in0 = __float_as_uint(f0) >> 31;  // the sign bit: NaN counts as inside
+            float t0 = 0.0f, t1 = 1.0f, t = 0.5f;
+            int side = 0;
+            for (uint32_t it = 0; it < root_iters; ++it) {
+                float tc = (t0 * f1 - t1 * f0) / (f1 - f0);
+                if (!(tc > t0 && tc < t1)) tc = 0.5f * (t0 + t1);  // NaN or degenerate: bisect
+                const float fc = eval<M>(s, ax + tc * ex, ay + tc * ey, az + tc * ez);
+                if ((__float_as_uint(fc) >> 31) == in0) {
+                    t0 = tc;
+                    f0 = fc;
+                    if (side == -1) f1 *= 0.5f;
+                    side = -1;
+                } else {
+                    t1 = tc;
+                    f1 = fc;
+                    if (side == 1) f0 *= 0.5f;
+                    side = 1;
+                }
+                t = tc;
+            }
+            sx += ax + t * ex;
+            sy += ay + t * ey;
+            sz += az + t * ez;
+        }
     }
     const float cf = (float)count;
     const float vx = __fadd_rn(0.0f, __fdiv_rn(sx, cf));

@@ -61,6 +61,12 @@ enum {
                                six extra estimator calls; polar Mandelbulb only (new) */
 };
 
+/* Edge crossings of the mesher. */
+enum {
+    CG_CROSSINGS_LERP = 0,  /* distance-weighted lerp of the corners, as buffer.rs:187-250 */
+    CG_CROSSINGS_ROOT = 1   /* the DE's root along the edge, regula falsi (new; issue #1) */
+};
+
 /* A shape; 48 bytes.  `power`/`max_iters`/`bailout` are Mandelbulb's fields
  * (src/shape/mandelbulb.rs:13-16; the reference's u64 max_iters fits u32 here). */
 typedef struct cg_shape {
@@ -144,6 +150,12 @@ void cg_mesher_destroy(cg_mesher* mesher);
  * positions, DE values and indices are unchanged, only the normals differ
  * from the reference's six-sample difference. */
 cg_status cg_mesher_set_normals(cg_mesher* mesher, uint32_t normals);
+/* Select the edge crossings (CG_CROSSINGS_LERP default).  CG_CROSSINGS_ROOT
+ * refines each crossing with `iters` (1..16) Illinois steps on the DE along
+ * the edge (iters extra estimator calls per crossing edge), the experiment
+ * buffer.rs:178-186 suggests; the cell table and index list are unchanged,
+ * vertex positions (and so their DE and normals) move onto the surface. */
+cg_status cg_mesher_set_crossings(cg_mesher* mesher, uint32_t crossings, uint32_t iters);
 
 /* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.
  * Writes min(count, cap) items; if a count exceeds its capacity the call

@@ -305,3 +305,37 @@ def test_empty_mesh_batch_and_device(cg, mesher):
     vv, ii = out.mesh(0)
     assert len(vv) == 0 and len(ii) == 0 and out.status == 0
     b.close()
+
+
+@pytest.mark.parametrize("shape_kind", ["p8", "polar"])
+def test_root_crossings(cg, shape_kind):
+    """Root-found crossings: same cells and indices as the reference's lerp,
+    every vertex stays in its cell, and the vertices sit much closer to the
+    surface (|DE at the vertex| drops)."""
+    s = cg.Mandelbulb(8, 15, 2.5) if shape_kind == "p8" else cg.MandelbulbPolar(8.3, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    res = 64
+    m = cg.Mesher(0)
+    try:
+        v0, i0, nv0, ni0, _ = m.generate(span, s, res, strict=False)
+        pts0 = m.last_points().cpu().numpy()
+        m.set_crossings("root", 6)
+        v1, i1, nv1, ni1, _ = m.generate(span, s, res, strict=False)
+        with pytest.raises(cg.CantucciError):
+            m.set_crossings("root", 0)
+    finally:
+        m.close()
+    assert (nv0, ni0) == (nv1, ni1)
+    assert np.array_equal(i0[:ni0], i1[:ni1])
+    a, b = as7(v0[:nv0]), as7(v1[:nv1])
+    # each vertex inside its (widened-span) cell
+    lo = np.asarray(span.start, np.float64) - (np.asarray(span.end) - np.asarray(span.start)) / res
+    step = (np.asarray(span.end, np.float64) - np.asarray(span.start)) * (res + 2) / res / res
+    cells = np.argwhere(pts0 != 0xFFFFFFFF)  # (x, y, z) in vertex-id order
+    order = pts0[cells[:, 0], cells[:, 1], cells[:, 2]].astype(np.int64)
+    cmin = lo + cells * step
+    ok = np.all((b[order, :3] >= cmin - 1e-5) & (b[order, :3] <= cmin + step + 1e-5), axis=1)
+    assert ok.mean() > 0.999
+    da, db = np.abs(a[:, 6]), np.abs(b[:, 6])
+    fin = np.isfinite(da) & np.isfinite(db)
+    assert np.median(db[fin]) < 0.5 * np.median(da[fin]), (np.median(db[fin]), np.median(da[fin]))
