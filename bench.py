@@ -38,8 +38,8 @@ FLOPS_PER_STEP = 76   # P=8 iteration: magnitude, dr, polynomial, + p (each op =
 FLOPS_PER_ESCAPE = 6  # the final magnitude of an escaping point
 FLOPS_PER_POINT = 4   # ln(r) * r, * 0.5, / dr
 # DRAM bytes of one k_de_grid_brick launch on the 513^3-corner span, from ncu:
-# 78,348,032 read + 560,385,024 written (algorithmic: 557,918,280 written).
-DE_TRAFFIC_RES512 = 78_348_032 + 560_385_024
+# 75,470,336 read + 554,948,096 written (algorithmic: 557,918,280 written).
+DE_TRAFFIC_RES512 = 75_470_336 + 554_948_096
 LAUNCHES_PER_MESH = 12  # k_de_grid_brick (sign words fused), k_cells, 3x scan, k_vertex_list,
 #                         k_place, k_quad_count, 3x scan, k_quad_emit (ncu launch list: 12 per mesh)
 
@@ -442,6 +442,18 @@ def run_extras(args, dev):
 
 
 # ---------------------------------------------------------------- GPU side
+def max_over_ranks(seconds: float, world: int, device) -> float:
+    """The slowest rank's time (an all-reduce MAX; NCCL on GPUs, gloo on CPU).
+    Replicas: each rank meshes its own copy of the workload, nothing else is
+    exchanged."""
+    if world <= 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _measured_hbm_gbs():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -503,12 +515,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
-    t_local = ms * 1e-3
-    t_max = t_local
-    if world > 1:
-        t = torch.tensor([t_local], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(ms * 1e-3, world, dev)
     value = world * n_pts * args.steps / t_max
 
     # End to end: the C ABI with host (pinned) output buffers.
@@ -518,6 +525,8 @@ def run_ours(args, rank, world, local_rank):
     idx_np = idx_h.numpy().view(np.uint32)
     mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np, strict=False)
     torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
     f0 = torch.cuda.Event(enable_timing=True)
     f1 = torch.cuda.Event(enable_timing=True)
     f0.record(stream)
@@ -525,11 +534,7 @@ def run_ours(args, rank, world, local_rank):
         mesher.generate(span, shape, res, vertices=verts_np, indices=idx_np, strict=False)
     f1.record(stream)
     f1.synchronize()
-    e2e_s = f0.elapsed_time(f1) * 1e-3
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(f0.elapsed_time(f1) * 1e-3, world, dev)
     clk = clocks.stop()
     e2e = {"value": world * n_pts * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": C.sizeof(_ffi.CgSpan) + C.sizeof(_ffi.CgShape),
