@@ -7,17 +7,32 @@
 #include "adjoint.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
+#include "point_io.cuh"
 
 namespace cg {
 
+// One point's 8 outputs: two 16-byte stores when `out` is 16-byte aligned.
+__device__ __forceinline__ void store8(float* __restrict__ out, uint64_t i, const float (&o)[8]) {
+    float* dst = out + 8 * i;
+    if ((((uintptr_t)out) & 15u) == 0) {
+        reinterpret_cast<float4*>(dst)[0] = make_float4(o[0], o[1], o[2], o[3]);
+        reinterpret_cast<float4*>(dst)[1] = make_float4(o[4], o[5], o[6], o[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = o[k];
+    }
+}
+
 __global__ void __launch_bounds__(128) k_de_grad(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
                                                  uint64_t n, float* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    __shared__ __align__(16) float stage[4][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
         float o[8];
-        polar_de_grad(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) out[8 * i + k] = o[k];
+        polar_de_grad(s, dm.m, x, y, z, o);
+        store8(out, base + (threadIdx.x & 31), o);
     }
 }
 
@@ -25,12 +40,14 @@ template <int T>
 __global__ void __launch_bounds__(128) k_de_grad_tangent(ShapeDev s, Dm3 dm,
                                                          const float* __restrict__ pts, uint64_t n,
                                                          float* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    __shared__ __align__(16) float stage[4][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
         float o[8];
-        polar_de_tangent<T>(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
-#pragma unroll
-        for (int k = 0; k < 8; ++k) out[8 * i + k] = o[k];
+        polar_de_tangent<T>(s, dm.m, x, y, z, o);
+        store8(out, base + (threadIdx.x & 31), o);
     }
 }
 
@@ -74,9 +91,12 @@ __global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float*
 template <int M>
 __global__ void __launch_bounds__(128) k_fd_grad(ShapeDev s, const float* __restrict__ pts,
                                                  uint64_t n, float h, float* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+    __shared__ __align__(16) float stage[4][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
+        const uint64_t i = base + (threadIdx.x & 31);
         float g[3];
 #pragma unroll 1
         for (int a = 0; a < 3; ++a) {

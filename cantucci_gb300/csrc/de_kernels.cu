@@ -5,16 +5,19 @@
 #include "common.cuh"
 #include "de.cuh"
 #include "kernels.cuh"
+#include "point_io.cuh"
 
 namespace cg {
 
 template <int M>
 __global__ void __launch_bounds__(256) k_de_points(ShapeDev s, const float* __restrict__ pts,
                                                    uint64_t n, float* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
-        out[i] = eval<M>(s, x, y, z);
+    __shared__ __align__(16) float stage[8][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z))
+            out[base + (threadIdx.x & 31)] = eval<M>(s, x, y, z);
     }
 }
 
@@ -104,28 +107,33 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
     }
 }
 
-__global__ void k_state(ShapeDev s, const float* __restrict__ pts, uint64_t n,
-                        float4* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+__global__ void __launch_bounds__(256) k_state(ShapeDev s, const float* __restrict__ pts,
+                                               uint64_t n, float4* __restrict__ out) {
+    __shared__ __align__(16) float stage[8][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
         MbState st;
         if (s.power == 8)
-            mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, pts[3 * i], pts[3 * i + 1],
-                                       pts[3 * i + 2], &st);
+            mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z, &st);
         else
-            mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, pts[3 * i],
-                                        pts[3 * i + 1], pts[3 * i + 2], &st);
-        out[i] = make_float4(st.r, st.dr, __uint_as_float(st.steps), __uint_as_float(st.escaped));
+            mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z, &st);
+        out[base + (threadIdx.x & 31)] =
+            make_float4(st.r, st.dr, __uint_as_float(st.steps), __uint_as_float(st.escaped));
     }
 }
 
 // Shape::contains (src/shape/mod.rs:78-80); Sphere overrides it with
 // |c - p|^2 <= r^2 (src/shape/sphere.rs:24-26).
-__global__ void k_contains(ShapeDev s, const float* __restrict__ pts, uint64_t n,
-                           uint8_t* __restrict__ out) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+__global__ void __launch_bounds__(256) k_contains(ShapeDev s, const float* __restrict__ pts,
+                                                  uint64_t n, uint8_t* __restrict__ out) {
+    __shared__ __align__(16) float stage[8][96];
+    const WarpWalk w = warp_walk();
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
+        const uint64_t i = base + (threadIdx.x & 31);
         bool in;
         if (s.kind == CG_SHAPE_SPHERE) {
             const float dx = __fsub_rn(s.center[0], x), dy = __fsub_rn(s.center[1], y),
