@@ -191,7 +191,7 @@ def _time_cuda(fn, reps=3, warm=1, stream=None):
     return e0.elapsed_time(e1) / reps
 
 
-def extra_batched(dev):
+def extra_batched(dev, cpu=True):
     """4096 seeded octree spans (res 8..64): one batch replayed from a CUDA
     graph vs one cg_generate_for_box_device call per span."""
     import numpy as np
@@ -212,22 +212,24 @@ def extra_batched(dev):
     ms_direct = _time_cuda(lambda: b.run(shape, graph=False), reps=3, warm=1)
     out = b.run(shape, graph=True)
     _, tot = out.host()
-    # the CPU builder (oracle restatement of generate_for_box) on every span,
-    # one span per host thread, and index lists compared on a sample
-    import oracle
-    oshape = oracle.mandelbulb(power, iters, 2.5)
-    oracle.lib()
-    threads = os.cpu_count() or 1
+    cpu_s, threads, same = None, os.cpu_count() or 1, None
+    if cpu:
+        # the CPU builder (oracle restatement of generate_for_box) on every
+        # span, one span per host thread, and index lists compared on a sample
+        import oracle
+        oshape = oracle.mandelbulb(power, iters, 2.5)
+        oracle.lib()
 
-    def cpu_one(j):
-        r = oracle.generate_for_box(oshape, spans[j].astype(np.float32), int(res[j]), nthreads=1,
-                                    vcap=int(res[j]) ** 3, icap=18 * int(res[j]) ** 3)
-        return r
-    t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        cpu = list(ex.map(cpu_one, range(len(res))))
-    cpu_s = time.perf_counter() - t0
-    same = sum(int(np.array_equal(out.mesh(j)[1], cpu[j]["indices"])) for j in range(0, len(res), 16))
+        def cpu_one(j):
+            return oracle.generate_for_box(oshape, spans[j].astype(np.float32), int(res[j]),
+                                           nthreads=1, vcap=int(res[j]) ** 3,
+                                           icap=18 * int(res[j]) ** 3)
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            cpu_res = list(ex.map(cpu_one, range(len(res))))
+        cpu_s = time.perf_counter() - t0
+        same = sum(int(np.array_equal(out.mesh(j)[1], cpu_res[j]["indices"]))
+                   for j in range(0, len(res), 16))
     m = cg.Mesher(dev)
     v = torch.empty((64 ** 3, 7), dtype=torch.float32, device=dev)
     i = torch.empty(18 * 64 ** 3, dtype=torch.int32, device=dev)
@@ -244,8 +246,11 @@ def extra_batched(dev):
             "default_tuning": default_tuning, "tuning": tuned["tuning"],
             "autotune_s": tune_s,
             "cpu_builder_s": cpu_s, "cpu_builder_threads": threads,
-            "cpu_builder_spans_per_s": 4096 / cpu_s, "speedup_vs_cpu_builder": cpu_s / (ms_graph * 1e-3),
-            "index_lists_equal_cpu_builder": "%d of %d sampled spans" % (same, len(range(0, len(res), 16))),
+            "cpu_builder_spans_per_s": 4096 / cpu_s if cpu_s else None,
+            "speedup_vs_cpu_builder": cpu_s / (ms_graph * 1e-3) if cpu_s else None,
+            "index_lists_equal_cpu_builder": ("%d of %d sampled spans" %
+                                              (same, len(range(0, len(res), 16)))
+                                              if cpu_s else None),
             "spans_per_s": 4096 / (ms_graph * 1e-3), "corners_per_s": corners / (ms_graph * 1e-3),
             "per_span_launches_s": seq_s, "per_span_spans_per_s": 4096 / seq_s,
             "speedup_vs_per_span": seq_s / (ms_graph * 1e-3)}
@@ -273,7 +278,7 @@ def band_points(shape, n, seed=1, oversample=6):
     return torch.cat(keep)[:n].contiguous()
 
 
-def extra_normals(dev, n=16 << 20):
+def extra_normals(dev, n=16 << 20, cpu=True):
     """Adjoint normals vs six-evaluation central differences on 16M band
     points (polar form, power 8, max_iters 15), with angular errors against
     the FP64 forward-mode oracle on a 2000-point subsample."""
@@ -301,6 +306,8 @@ def extra_normals(dev, n=16 << 20):
            "modes": "adjoint = reverse mode with checkpoint recompute (DE, grad, d/dpower, "
                     "d/drotation); tangent_normals = forward mode along x, y, z (DE, grad, "
                     "d/drotation); tangent_all = forward mode with the power direction too"}
+    if not cpu:
+        return out
     try:
         import oracle
         sub = pts[:2000]
@@ -429,13 +436,64 @@ def extra_polar_mesh_normals(dev, res=RES):
     return out
 
 
+def extra_fp64_check(dev, res=RES, stride=67):
+    """Distances of the 513^3 span against the FP64 oracle on every 67th
+    corner (~2M points): sign agreement, the share within 1e-5 relative and
+    1e-6 absolute, and how many of the points outside 1e-5 relative escape
+    at a different iteration than in FP64."""
+    import numpy as np
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import _ffi, workloads as W
+    import oracle
+    shape = cg.Mandelbulb(**SHAPE)
+    span = cg.Span(*W.SPAN_C1)
+    n = res + 1
+    d32 = shape.span_grid(span, res).reshape(-1)
+    idx = torch.arange(0, n ** 3, stride, device=d32.device)
+    d32 = d32[idx].cpu().numpy().astype(np.float64)
+    # corner coordinates exactly as the kernels form them (f32, v / res exact)
+    rf = np.float32(res)
+    st = (span.start + -((span.end - span.start) / rf)).astype(np.float32)
+    en = (span.end + (span.end - span.start) / rf).astype(np.float32)
+    across = (en - st).astype(np.float32)
+    ii = idx.cpu().numpy()
+    v = np.stack([ii // (n * n), (ii // n) % n, ii % n], 1).astype(np.float32)
+    pts = (st + across * (v * (np.float32(1.0) / rf))).astype(np.float32)
+    pd = torch.as_tensor(pts).to(dev)
+    state = torch.empty((len(pts), 4), dtype=torch.float32, device=dev)
+    _ffi.check(_ffi.load().cg_mandelbulb_state(C.byref(shape._cshape()), C.c_void_p(pd.data_ptr()),
+                                               len(pts), C.c_void_p(state.data_ptr()), None))
+    steps32 = state.cpu().numpy()[:, 2].view(np.uint32)
+    d64, steps64 = oracle.de_f64(oracle.mandelbulb(**SHAPE), pts, with_steps=True)
+    fin = np.isfinite(d64) & np.isfinite(d32)
+    rel_ok = np.abs(d32 - d64) <= 1e-5 * np.abs(d64)
+    out_rel = fin & ~rel_ok
+    return {"workload": "every %dth corner of the 513^3 span (%d points)" % (stride, len(pts)),
+            "sign_agreement": float(np.mean(np.signbit(d32[fin]) == np.signbit(d64[fin]))),
+            "frac_within_1e-5_rel": float(np.mean(rel_ok[fin])),
+            "frac_within_1e-6_abs": float(np.mean(np.abs(d32[fin] - d64[fin]) <= 1e-6)),
+            "outside_1e-5_rel": int(out_rel.sum()),
+            "outside_with_other_escape_step": int((out_rel & (steps32 != steps64)).sum()),
+            "non_finite": int((~fin).sum())}
+
+
 def run_extras(args, dev):
+    """The other configurations.  The oracle runs only in CPU legs (the CPU
+    builder's timing and the accuracy checks against FP64), which
+    --no-cpu-baseline switches off together with the cpu_baseline leg."""
+    cpu = not args.no_cpu_baseline
     out = {}
-    for name, fn in (("de_variants", extra_de_variants), ("batched_spans", extra_batched),
-                     ("normals", extra_normals), ("polar_mesh_normals", extra_polar_mesh_normals),
-                     ("depth_fit", extra_depth_fit)):
+    legs = [("de_variants", lambda: extra_de_variants(dev)),
+            ("batched_spans", lambda: extra_batched(dev, cpu)),
+            ("normals", lambda: extra_normals(dev, cpu=cpu)),
+            ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
+            ("depth_fit", lambda: extra_depth_fit(dev))]
+    if cpu:
+        legs.insert(1, ("fp64_check", lambda: extra_fp64_check(dev)))
+    for name, fn in legs:
         try:
-            out[name] = fn(dev)
+            out[name] = fn()
         except Exception as e:  # report, never hide the headline number
             out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
     return out
@@ -610,6 +668,7 @@ def run_ours(args, rank, world, local_rank):
                                "factor is NaN and src/math.rs:19 asserts; the mesh is "
                                "completed with factor 0 there, like the oracle"},
         "de_kernel_pts_per_s": n_pts / (de_ms * 1e-3),
+        "cells_per_s": world * res ** 3 * args.steps / t_max,
         "roofline": roofline, "e2e": e2e, "clocks": clk,
         "gpu_launches": LAUNCHES_PER_MESH * args.steps,
     }
