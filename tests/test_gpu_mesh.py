@@ -339,3 +339,38 @@ def test_root_crossings(cg, shape_kind):
     da, db = np.abs(a[:, 6]), np.abs(b[:, 6])
     fin = np.isfinite(da) & np.isfinite(db)
     assert np.median(db[fin]) < 0.5 * np.median(da[fin]), (np.median(db[fin]), np.median(da[fin]))
+
+
+@pytest.mark.slow
+def test_max_resolution_span(cg):
+    """Resolution 1024 (the largest the ABI takes: 1025^3 corners, a 4.3 GB
+    distance grid): the mesh completes, every index refers to a vertex, and
+    sampled corners of the grid equal the point estimator at the same
+    coordinates bit for bit."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span([-1.2] * 3, [1.2] * 3)
+    res = 1024
+    m = cg.Mesher(0)
+    try:
+        vcap, icap = 24 << 20, 160 << 20
+        v = torch.empty((vcap, 7), dtype=torch.float32, device="cuda")
+        i = torch.empty(icap, dtype=torch.int32, device="cuda")
+        nv, ni, tm = m.generate_device(span, s, res, v, i, strict=False)
+        assert m.last_status in (0, 3)  # OK or the reference's lerp panic (completed)
+        assert 0 < nv <= vcap and 0 < ni <= icap and ni % 6 == 0
+        idx = i[:ni].to(torch.int64) & 0xFFFFFFFF
+        assert int(idx.max()) < nv
+        d = m.last_dists()
+        n = res + 1
+        rng = np.random.default_rng(11)
+        cells = rng.integers(0, n, size=(10000, 3))
+        rf = np.float32(res)
+        st = (span.start + -((span.end - span.start) / rf)).astype(np.float32)
+        en = (span.end + (span.end - span.start) / rf).astype(np.float32)
+        pts = (st + (en - st) * (cells.astype(np.float32) * (np.float32(1) / rf))).astype(np.float32)
+        want = s.batch_min_distance_from(pts)
+        got = d[cells[:, 0], cells[:, 1], cells[:, 2]].cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    finally:
+        m.close()
