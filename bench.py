@@ -478,13 +478,54 @@ def extra_fp64_check(dev, res=RES, stride=67):
             "non_finite": int((~fin).sum())}
 
 
+def extra_small_span(dev, reps=50):
+    """Config 1: the 65^3-corner span (res 64, the reference's leaf
+    resolution) meshed alone, device outputs and pinned host outputs: a
+    latency-bound call (12 kernels on 274,625 corners)."""
+    import numpy as np
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    span = cg.Span(*W.SPAN_C1)
+    shape = cg.Mandelbulb(**SHAPE)
+    res = 64
+    m = cg.Mesher(dev)
+    v = torch.empty((res ** 3 // 4, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(18 * res ** 3 // 4, dtype=torch.int32, device=dev)
+    vh = torch.empty((res ** 3 // 4, 7), dtype=torch.float32, pin_memory=True)
+    ih = torch.empty(18 * res ** 3 // 4, dtype=torch.int32, pin_memory=True)
+    vnp = vh.numpy().view(cg.VERTEX_DTYPE).reshape(-1)
+    inp = ih.numpy().view(np.uint32)
+    try:
+        for _ in range(5):
+            m.generate_device(span, shape, res, v, i)
+            m.generate(span, shape, res, vertices=vnp, indices=inp)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            nv, ni, _ = m.generate_device(span, shape, res, v, i)
+        dev_s = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            m.generate(span, shape, res, vertices=vnp, indices=inp)
+        host_s = (time.perf_counter() - t0) / reps
+    finally:
+        m.close()
+    n = (res + 1) ** 3
+    return {"workload": "single span [-1.2,1.2]^3 at res 64 (274,625 corners), P=8, max_iters 15",
+            "vertices": nv, "indices": ni,
+            "device_call_ms": 1e3 * dev_s, "device_corners_per_s": n / dev_s,
+            "host_call_ms": 1e3 * host_s, "host_corners_per_s": n / host_s,
+            "timing": "host wall clock per synchronous call, %d calls" % reps}
+
+
 def run_extras(args, dev):
     """The other configurations.  The oracle runs only in CPU legs (the CPU
     builder's timing and the accuracy checks against FP64), which
     --no-cpu-baseline switches off together with the cpu_baseline leg."""
     cpu = not args.no_cpu_baseline
     out = {}
-    legs = [("de_variants", lambda: extra_de_variants(dev)),
+    legs = [("small_span", lambda: extra_small_span(dev)),
+            ("de_variants", lambda: extra_de_variants(dev)),
             ("batched_spans", lambda: extra_batched(dev, cpu)),
             ("normals", lambda: extra_normals(dev, cpu=cpu)),
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
