@@ -145,6 +145,7 @@ struct cg_mesher {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // host-output copies overlapping placement
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join = nullptr;  // quads on copy_stream beside placement
     char* work = nullptr;
     size_t work_bytes = 0;
     cg_vertex* dverts = nullptr;
@@ -205,10 +206,11 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
     CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
+    const SideStream side = {m->copy_stream, m->fork, m->join};
     CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
                                   /*signs_ready=*/true,
                                   /*analytic_normals=*/m->normals == CG_NORMALS_ADJOINT,
-                                  m->root_iters));
+                                  m->root_iters, &side));
     CG_CUDA(cudaEventRecord(m->ev[3], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -273,20 +275,20 @@ cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* sh
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
     CG_CUDA(cudaStreamSynchronize(m->copy_stream));
-    m->last_res = res;
-    m->last_w = w;
     if (tm) {
-        float a = 0, b = 0, c = 0, e = 0;
+        // The quads ran on the copy stream from ev[2]; ev[3] closes them.
+        float a = 0, b = 0, c = 0;
         CG_CUDA(cudaEventElapsedTime(&a, m->ev[0], m->ev[1]));
-        CG_CUDA(cudaEventElapsedTime(&b, m->ev[1], m->ev[2]));
+        CG_CUDA(cudaEventElapsedTime(&b, m->ev[1], m->ev[4]));
         CG_CUDA(cudaEventElapsedTime(&c, m->ev[2], m->ev[3]));
-        CG_CUDA(cudaEventElapsedTime(&e, m->ev[3], m->ev[4]));
         tm->first_ms = a;
-        tm->second_ms = b + e;  // cells, counts and vertex placement
-        tm->third_ms = c;       // quad indices
+        tm->second_ms = b;  // cells, counts and vertex placement
+        tm->third_ms = c;   // quad indices, beside the placement
         tm->vertices = m->hcnt->vertices;
         tm->faces = m->hcnt->quads;
     }
+    m->last_res = res;
+    m->last_w = w;
     return CG_OK;
 }
 
@@ -382,6 +384,8 @@ cg_status cg_mesher_create(int device, cg_mesher** out) {
         return st;
     }
     for (auto& e : m->ev) cudaEventCreate(&e);
+    cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming);
     if ((st = cuda_status(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking),
                           "cudaStreamCreate", __FILE__, __LINE__)) != CG_OK) {
         cg_mesher_destroy(m);
@@ -406,6 +410,8 @@ void cg_mesher_destroy(cg_mesher* m) {
     if (m->hcnt) cudaFreeHost(m->hcnt);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
+    if (m->fork) cudaEventDestroy(m->fork);
+    if (m->join) cudaEventDestroy(m->join);
     if (m->copy_stream) cudaStreamDestroy(m->copy_stream);
     if (m->stream) cudaStreamDestroy(m->stream);
     delete m;

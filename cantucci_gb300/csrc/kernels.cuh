@@ -88,17 +88,25 @@ size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 // their capacity; counts land in w.counters.  analytic_normals (polar form
 // only) replaces the six-sample normal by the forward-mode gradient;
 // root_iters > 0 places edge crossings at the DE's root along each edge.
+// A second stream and a fork / join event pair: with it the quad indices
+// are built concurrently with the vertex placement.
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
 cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals = false, uint32_t root_iters = 0);
+                                 bool analytic_normals = false, uint32_t root_iters = 0,
+                                 const SideStream* side = nullptr);
 
 // The same steps for a mesh whose outputs go to host memory, reordered so
 // the transfers overlap the vertex placement: surface cells and both counts
 // first (read back: ev_counts is synchronised), then the quad indices into
-// `dev_idx` with their device-to-host copy on `copy_st`, then the vertices,
-// which k_place stores straight into `host_verts` (pinned, device-mapped).
+// `dev_idx` and their device-to-host copy on `copy_st` (ev_quads marks the
+// end of the indices), while on `st` k_place stores the vertices straight
+// into `host_verts` (pinned, device-mapped).
 cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                               const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
                               uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,

@@ -271,8 +271,22 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals, uint32_t root_iters) {
+                                 bool analytic_normals, uint32_t root_iters,
+                                 const SideStream* side) {
     CG_TRY(launch_cells(d, w, st, signs_ready));
+    if (side) {
+        // The quads need only the cell table and the signs: they run on the
+        // side stream while the (compute-bound) vertex placement runs here.
+        CG_CUDA(cudaEventRecord(side->fork, st));
+        CG_CUDA(cudaStreamWaitEvent(side->stream, side->fork, 0));
+        CG_TRY(launch_quad_count(d, w, side->stream));
+        CG_TRY(launch_quad_emit(d, w, idx, icap, side->stream));
+        CG_CUDA(cudaEventRecord(side->join, side->stream));
+        CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals, root_iters));
+        if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
+        CG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
+        return CG_OK;
+    }
     CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals, root_iters));
     if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
     CG_TRY(launch_quad_count(d, w, st));
@@ -293,9 +307,10 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     CG_CUDA(cudaEventSynchronize(ev_counts));
     const uint64_t ni = 6ull * hcnt->quads;
     const uint64_t ci = ni < icap ? ni : icap;
-    CG_TRY(launch_quad_emit(d, w, dev_idx, icap, st));
-    CG_CUDA(cudaEventRecord(ev_quads, st));
-    CG_CUDA(cudaStreamWaitEvent(copy_st, ev_quads, 0));
+    // The quads and their copy on copy_st, beside the placement on st.
+    CG_CUDA(cudaStreamWaitEvent(copy_st, ev_counts, 0));
+    CG_TRY(launch_quad_emit(d, w, dev_idx, icap, copy_st));
+    CG_CUDA(cudaEventRecord(ev_quads, copy_st));
     if (ci)
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 copy_st));

@@ -260,6 +260,9 @@ struct cg_batch {
     uint32_t cap_jobs = 0;
     uint64_t cap_dist = 0, cap_sgnw = 0, cap_cw = 0, cap_rows = 0;
     uint32_t plan_gen = 0;  // bumped by cg_batch_set_jobs (graphs recapture)
+    // quads are built on `side` beside the vertex placement
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cg_batch_tuning tune = {256, 64, 32, 128};
     uint32_t planned_brick_min_res = 0;  // the threshold the device table holds
     // graph cache
@@ -472,6 +475,14 @@ cg_status cg_batch_create(int device, const cg_span_job* host_jobs, uint32_t n_j
         return st;
     }
     b->hjobs = std::move(jobs);
+    if (cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        cg_batch_destroy(b);
+        set_error("cudaStreamCreate / cudaEventCreate failed");
+        return CG_ECUDA;
+    }
     *out = b;
     return CG_OK;
 }
@@ -480,6 +491,9 @@ void cg_batch_destroy(cg_batch* b) {
     if (!b) return;
     DeviceScope g(b->device);
     if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->work) cudaFree(b->work);
     delete b;
 }
@@ -571,18 +585,28 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     k_batch_vertex_list<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->cellbits, b->wordoff,
                                            b->rowoff, vertex_cap, b->cellidx, b->celljob);
     CG_CHECK_LAUNCH("k_batch_vertex_list");
+    // Quads (cell table and signs only) on the side stream, beside the
+    // compute-bound placement.
+    cudaStream_t qs = st;
+    if (b->side) {
+        CG_CUDA(cudaEventRecord(b->fork, st));
+        CG_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
+        qs = b->side;
+    }
+    k_batch_quad_count<<<G, 256, 0, qs>>>(b->jobs, b->njobs, b->rows, b->sgn, b->quadcnt);
+    CG_CHECK_LAUNCH("k_batch_quad_count");
+    CG_TRY(launch_exclusive_scan(b->quadcnt, b->quadoff, b->rows, b->scratch, &b->tot->quads, qs));
+    k_batch_quad_emit<<<G, 256, 0, qs>>>(b->jobs, b->njobs, b->rows, b->sgn, b->dists, b->cellbits,
+                                         b->wordoff, b->rowoff, b->quadoff, indices, index_cap);
+    CG_CHECK_LAUNCH("k_batch_quad_emit");
+    if (b->side) CG_CUDA(cudaEventRecord(b->join, b->side));
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
     case MODE_P8: CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st)); break;
     case MODE_INT: CG_TRY(launch_batch_place<MODE_INT>(b, s, vertices, vertex_cap, st)); break;
     case MODE_POLAR: CG_TRY(launch_batch_place<MODE_POLAR>(b, s, vertices, vertex_cap, st)); break;
     default: CG_TRY(launch_batch_place<MODE_SPHERE>(b, s, vertices, vertex_cap, st)); break;
     }
-    k_batch_quad_count<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->quadcnt);
-    CG_CHECK_LAUNCH("k_batch_quad_count");
-    CG_TRY(launch_exclusive_scan(b->quadcnt, b->quadoff, b->rows, b->scratch, &b->tot->quads, st));
-    k_batch_quad_emit<<<G, 256, 0, st>>>(b->jobs, b->njobs, b->rows, b->sgn, b->dists, b->cellbits,
-                                         b->wordoff, b->rowoff, b->quadoff, indices, index_cap);
-    CG_CHECK_LAUNCH("k_batch_quad_emit");
+    if (b->side) CG_CUDA(cudaStreamWaitEvent(st, b->join, 0));
     k_batch_results<<<grid_for(b->njobs, 256, 4), 256, 0, st>>>(b->jobs, b->njobs, b->rowoff,
                                                                  b->quadoff, b->tot, results);
     CG_CHECK_LAUNCH("k_batch_results");

@@ -97,7 +97,8 @@ typedef struct cg_vertex {
 typedef struct cg_timings {
     float first_ms;   /* step 1: distances at every corner */
     float second_ms;  /* step 2: surface cells, vertices, normals */
-    float third_ms;   /* step 3: quad indices */
+    float third_ms;   /* step 3: quad indices (built beside step 2's vertex placement on
+                         the GPU: this is the part that outlasts the placement) */
     uint32_t vertices;
     uint32_t faces;
 } cg_timings;
