@@ -518,6 +518,92 @@ def extra_small_span(dev, reps=50):
             "timing": "host wall clock per synchronous call, %d calls" % reps}
 
 
+def extra_lod(dev, cpu=True, updates=24):
+    """The level-of-detail driver on a camera flight towards the surface:
+    the camera moves from 3.0 to 1.25 from the origin along -y over 24
+    updates (each one waits for its batched run), res-64 leaves as in the
+    reference.  Reports the leaves meshed, the time per update, and the CPU
+    builder's time for the same jobs (one job per host thread)."""
+    import numpy as np
+    import cantucci_gb300 as cg
+    from cantucci_gb300.lod import Camera, ShapeMesh
+    shape = cg.Mandelbulb(**SHAPE)
+    sm = ShapeMesh(shape, resolution=64, device=dev)
+    jobs, times, splits = [], [], 0
+    seen = set()
+    try:
+        for k in range(updates):
+            y = -3.0 + (3.0 - 1.25) * k / (updates - 1)
+            cam = Camera(position=(0.05, y, 0.08), direction=(0.0, 1.0, 0.03))
+            t0 = time.perf_counter()
+            st = sm.update(cam, wait=True)
+            times.append(time.perf_counter() - t0)
+            splits += st["splits"]
+            for leaf in sm.leaves():
+                key = tuple(leaf.start.tolist()) + tuple(leaf.end.tolist())
+                if leaf.status == 1 and key not in seen:
+                    seen.add(key)
+                    jobs.append(np.concatenate([leaf.start, leaf.end]).astype(np.float32))
+        final = sm.leaves()
+    finally:
+        sm.close()
+    out = {"workload": "camera from y=-3.0 to y=-1.25 over %d updates, Mandelbulb P=8 "
+                       "max_iters 15, res-64 leaves" % updates,
+           "updates": updates, "leaves_meshed": len(jobs), "splits": splits,
+           "final_leaves": len(final), "max_depth": max(l.depth for l in final),
+           "update_ms_mean": 1e3 * float(np.mean(times)),
+           "update_ms_max": 1e3 * float(np.max(times)),
+           "gpu_leaves_per_s": len(jobs) / float(np.sum(times))}
+    if cpu and jobs:
+        import oracle
+        oshape = oracle.mandelbulb(**SHAPE)
+        oracle.lib()
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            list(ex.map(lambda sp: oracle.generate_for_box(oshape, sp, 64, nthreads=1,
+                                                           vcap=64 ** 3, icap=18 * 64 ** 3),
+                        jobs))
+        cpu_s = time.perf_counter() - t0
+        out["cpu_builder_s"] = cpu_s
+        out["cpu_leaves_per_s"] = len(jobs) / cpu_s
+        out["speedup_vs_cpu_builder"] = out["gpu_leaves_per_s"] / out["cpu_leaves_per_s"]
+    return out
+
+
+def extra_root_crossings(dev, res=RES):
+    """The 513^3 span meshed with the reference's lerped crossings and with
+    root-found crossings (4 Illinois steps per crossing edge): mesh time and
+    the median |DE| at the vertices."""
+    import numpy as np
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    span = cg.Span(*W.SPAN_C1)
+    shape = cg.Mandelbulb(**SHAPE)
+    vcap, icap = res ** 3 // 16, 18 * res ** 3 // 16
+    v = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(icap, dtype=torch.int32, device=dev)
+    out = {"workload": "Mandelbulb P=8 max_iters 15, %d^3 corners" % (res + 1)}
+    m = cg.Mesher(dev)
+    try:
+        for mode in ("lerp", "root"):
+            m.set_crossings(mode, 4)
+            m.generate_device(span, shape, res, v, i, strict=False)
+            best = None
+            for _ in range(3):
+                nv, ni, tm = m.generate_device(span, shape, res, v, i, strict=False)
+                ms = tm.first_ms + tm.second_ms + tm.third_ms
+                best = ms if best is None else min(best, ms)
+            de = v[:nv, 6].abs()
+            de = de[torch.isfinite(de)]
+            out[mode] = {"mesh_ms": best, "vertices": nv,
+                         "median_abs_de_at_vertex": float(de.median())}
+    finally:
+        m.close()
+    out["de_ratio"] = out["root"]["median_abs_de_at_vertex"] / out["lerp"]["median_abs_de_at_vertex"]
+    return out
+
+
 def run_extras(args, dev):
     """The other configurations.  The oracle runs only in CPU legs (the CPU
     builder's timing and the accuracy checks against FP64), which
@@ -529,6 +615,8 @@ def run_extras(args, dev):
             ("batched_spans", lambda: extra_batched(dev, cpu)),
             ("normals", lambda: extra_normals(dev, cpu=cpu)),
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
+            ("root_crossings", lambda: extra_root_crossings(dev)),
+            ("lod", lambda: extra_lod(dev, cpu)),
             ("depth_fit", lambda: extra_depth_fit(dev))]
     if cpu:
         legs.insert(1, ("fp64_check", lambda: extra_fp64_check(dev)))
