@@ -617,9 +617,11 @@ def run_extras(args, dev):
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
             ("root_crossings", lambda: extra_root_crossings(dev)),
             ("lod", lambda: extra_lod(dev, cpu)),
-            ("depth_fit", lambda: extra_depth_fit(dev))]
+            ("depth_fit", lambda: extra_depth_fit(dev, args.fit_steps))]
     if cpu:
         legs.insert(1, ("fp64_check", lambda: extra_fp64_check(dev)))
+    if args.only_extra:
+        legs = [(n, f) for n, f in legs if n == args.only_extra]
     for name, fn in legs:
         try:
             out[name] = fn()
@@ -823,6 +825,10 @@ def main():
     ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3],
                     help="step-1 kernel: 0 auto (2x4x4 bricks), 1 linear, 2 bricks, 3 packed "
                          "f32x2 (all bit-identical)")
+    ap.add_argument("--fit-steps", type=int, default=300,
+                    help="Adam steps of the depth-map fit extra")
+    ap.add_argument("--only-extra", default=None,
+                    help="run just this one of the extra measurements (e.g. depth_fit)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batched, normals and depth-map measurements")
     ap.add_argument("--traffic", type=float, default=None,

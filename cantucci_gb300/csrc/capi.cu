@@ -535,6 +535,7 @@ cg_status cg_set_option(const char* name, int64_t value) {
     if (name && strcmp(name, "de_grid_kernel") == 0 && set_de_grid_kernel((int)value))
         return CG_OK;
     if (name && set_batch_option(name, value)) return CG_OK;
+    if (name && set_trace_option(name, value)) return CG_OK;
     set_error("unknown option or value: %s = %lld", name ? name : "(null)", (long long)value);
     return CG_EINVAL;
 }

@@ -49,6 +49,8 @@ cg_status launch_contains(const ShapeDev& s, const float* pts, uint64_t n, uint8
                           cudaStream_t st);
 cg_status launch_march(const ShapeDev& s, const float* org, const float* dir, uint64_t n,
                        uint32_t max_steps, float eps, float* hits, uint8_t* hit, cudaStream_t st);
+// cg_set_option knobs of the depth-map march (trace.cu).
+int set_trace_option(const char* name, int64_t v);
 // Shape argument checks of the C ABI (kind, power, max_iters).
 cg_status check_shape(const cg_shape* s);
 

@@ -12,6 +12,7 @@
 // both gradients at x; the kernel sums dL/dt * dt/dtheta over pixels for
 // theta = (power, three Euler angles).
 #include <cmath>
+#include <cstring>
 
 #include "adjoint.cuh"
 #include "common.cuh"
@@ -59,6 +60,109 @@ __global__ void __launch_bounds__(128) k_trace(ShapeDev s, CameraDev c, uint32_t
             if (t > 10.0f) break;
         }
         depth[i] = out;
+    }
+}
+
+// The polar estimator one loop iteration at a time (the same operations as
+// polar_de), so that a lane can start a new estimate while its warp
+// neighbours are still iterating theirs.
+struct PolarIter {
+    float qx, qy, qz;  // R^T p
+    StepState st;      // z, dr
+    float r;
+    uint32_t it;
+
+    __device__ __forceinline__ void start(const ShapeDev& s, float px, float py, float pz) {
+        qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+        qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+        qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+        st = {qx, qy, qz, 1.0f};
+        r = 0.0f;
+        it = 0;
+    }
+    // One iteration; true when the estimate is complete (escape, or the
+    // last iteration ran: r is then the stale |z| of that iteration).
+    __device__ __forceinline__ bool advance(const ShapeDev& s) {
+        float ri;
+        if (!polar_step(s, qx, qy, qz, st, ri)) {
+            r = ri;
+            return true;
+        }
+        r = ri;
+        return ++it >= s.max_iters;
+    }
+    __device__ __forceinline__ float value() const {
+        const float ln_r = __fmul_rn(logf(r), r);
+        return x86_nan(__fdiv_rn(__fmul_rn(0.5f, ln_r), st.dr));
+    }
+};
+
+// The same march with a work queue: persistent warps, and a lane whose ray
+// is finished takes the next pixel at once (one atomic per warp and refill),
+// so a warp no longer waits for its longest ray.  For the polar form the
+// lanes advance one estimator iteration per loop trip, so a lane also does
+// not wait for the slowest estimate of its warp.  Same depths as k_trace.
+template <int M>
+__global__ void __launch_bounds__(128) k_trace_queue(ShapeDev s, CameraDev c, uint32_t max_steps,
+                                                     float eps_scale, float* __restrict__ depth,
+                                                     uint32_t* __restrict__ next) {
+    const uint32_t n = c.width * c.height;
+    const float pix = 2.0f * c.tan_half / c.height;
+    const uint32_t lane = threadIdx.x & 31;
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    uint32_t i = kNone, k = 0;
+    bool done = false;
+    float d[3] = {0.0f, 0.0f, 0.0f}, t = 0.0f;
+    PolarIter pe;
+    for (;;) {
+        const bool need = !done && i == kNone;
+        const unsigned need_mask = __ballot_sync(0xFFFFFFFFu, need);
+        if (need_mask) {
+            const int leader = __ffs(need_mask) - 1;
+            uint32_t base = 0;
+            if ((int)lane == leader) base = atomicAdd(next, (uint32_t)__popc(need_mask));
+            base = __shfl_sync(0xFFFFFFFFu, base, leader);
+            if (need) {
+                const uint32_t idx = base + __popc(need_mask & ((1u << lane) - 1u));
+                if (idx >= n) {
+                    done = true;
+                } else if (max_steps == 0) {
+                    depth[idx] = -1.0f;
+                } else {
+                    i = idx;
+                    pixel_ray(c, i, d);
+                    t = 0.0f;
+                    k = 0;
+                    if (M == MODE_POLAR) pe.start(s, c.eye[0], c.eye[1], c.eye[2]);
+                }
+            }
+        }
+        if (__all_sync(0xFFFFFFFFu, done)) break;
+        if (done || i == kNone) continue;
+        float de;
+        if (M == MODE_POLAR) {
+            if (!pe.advance(s)) continue;
+            de = pe.value();
+        } else {
+            de = eval<M>(s, c.eye[0] + t * d[0], c.eye[1] + t * d[1], c.eye[2] + t * d[2]);
+        }
+        float out = -1.0f;
+        bool fin = false;
+        if (!(de == de)) {
+            fin = true;  // NaN: no surface information
+        } else if (de < eps_scale * fmaxf(t, 1e-3f) * pix) {
+            out = t;
+            fin = true;
+        } else {
+            t += de;
+            fin = t > 10.0f || ++k >= max_steps;
+        }
+        if (fin) {
+            depth[i] = out;
+            i = kNone;
+        } else if (M == MODE_POLAR) {
+            pe.start(s, c.eye[0] + t * d[0], c.eye[1] + t * d[1], c.eye[2] + t * d[2]);
+        }
     }
 }
 
@@ -119,6 +223,27 @@ static CameraDev make_camera(const cg_camera& cam) {
     return c;
 }
 
+// "trace_kernel": 1 (default) the work-queue march, 0 one pixel per thread.
+static int g_trace_kernel = 1;
+
+int set_trace_option(const char* name, int64_t v) {
+    if (strcmp(name, "trace_kernel") || v < 0 || v > 1) return 0;
+    g_trace_kernel = (int)v;
+    return 1;
+}
+
+template <int M>
+static void launch_trace_queue(const ShapeDev& s, const CameraDev& c, uint32_t max_steps,
+                               float eps_scale, float* depth, uint32_t* next, cudaStream_t st) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue<M>, 128, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    k_trace_queue<M><<<(unsigned)(sm_count() * per_sm), 128, 0, st>>>(s, c, max_steps, eps_scale,
+                                                                     depth, next);
+}
+
 static cg_status check_camera(const cg_camera* cam) {
     if (!cam || cam->width == 0 || cam->height == 0 || !(cam->fov_y > 0.0f && cam->fov_y < 3.1f) ||
         (uint64_t)cam->width * cam->height > (1ull << 31)) {
@@ -144,15 +269,30 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     const ShapeDev s = make_shape_dev(*shape);
     const CameraDev c = make_camera(*camera);
     const uint64_t n = (uint64_t)c.width * c.height;
-    const unsigned G = grid_for(n, 128, 16);
     cudaStream_t st = (cudaStream_t)stream;
-    switch (mode_of(s, CG_NUMERICS_EXACT)) {
-    case MODE_P8: k_trace<MODE_P8><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
-    case MODE_INT: k_trace<MODE_INT><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
-    case MODE_POLAR: k_trace<MODE_POLAR><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
-    default: k_trace<MODE_SPHERE><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+    if (g_trace_kernel == 0) {
+        const unsigned G = grid_for(n, 128, 16);
+        switch (mode_of(s, CG_NUMERICS_EXACT)) {
+        case MODE_P8: k_trace<MODE_P8><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+        case MODE_INT: k_trace<MODE_INT><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+        case MODE_POLAR: k_trace<MODE_POLAR><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+        default: k_trace<MODE_SPHERE><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+        }
+        CG_CHECK_LAUNCH("k_trace");
+        return CG_OK;
     }
-    CG_CHECK_LAUNCH("k_trace");
+    uint32_t* next = nullptr;
+    CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&next), sizeof(uint32_t), st));
+    CG_CUDA(cudaMemsetAsync(next, 0, sizeof(uint32_t), st));
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    case MODE_P8: launch_trace_queue<MODE_P8>(s, c, max_steps, eps_scale, depth, next, st); break;
+    case MODE_INT: launch_trace_queue<MODE_INT>(s, c, max_steps, eps_scale, depth, next, st); break;
+    case MODE_POLAR: launch_trace_queue<MODE_POLAR>(s, c, max_steps, eps_scale, depth, next, st); break;
+    default: launch_trace_queue<MODE_SPHERE>(s, c, max_steps, eps_scale, depth, next, st); break;
+    }
+    const cudaError_t le = cudaGetLastError();
+    CG_CUDA(cudaFreeAsync(next, st));
+    CG_CUDA(le);
     return CG_OK;
 }
 

@@ -132,3 +132,33 @@ def test_fit_reduces_loss(cg):
     assert losses[best] < 0.95 * losses[0], losses
     power_at = [8.0] + powers  # the callback runs after each step
     assert abs(power_at[best] - 8.3) < abs(8.0 - 8.3)
+
+
+@pytest.mark.parametrize("kind", ["polar", "p8", "sphere"])
+def test_queue_march_matches_per_pixel_march(cg, kind):
+    """The work-queue march (default) gives the per-pixel march's depths bit
+    for bit."""
+    import ctypes as C
+    import torch
+    from cantucci_gb300 import _ffi, fit
+    lib = _ffi.load()
+    cam = fit.camera(160, 120)
+    if kind == "polar":
+        shape = cg.MandelbulbPolar(8.3, 15, 2.5, (0.2, 0.1, 0.0))
+    elif kind == "p8":
+        shape = cg.Mandelbulb(8, 15, 2.5)
+    else:
+        shape = cg.Sphere((0.1, 0.0, -0.2), 0.9)
+    outs = []
+    try:
+        for k in (0, 1):
+            _ffi.check(lib.cg_set_option(b"trace_kernel", k))
+            d = torch.empty((cam.height, cam.width), dtype=torch.float32, device="cuda")
+            _ffi.check(lib.cg_trace_depth(C.byref(shape._cshape()), C.byref(cam), 256, 1e-4,
+                                          C.c_void_p(d.data_ptr()), None))
+            torch.cuda.synchronize()
+            outs.append(d.cpu().numpy())
+    finally:
+        lib.cg_set_option(b"trace_kernel", 1)
+    assert (outs[0] > 0).sum() > 1000
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
