@@ -766,6 +766,9 @@ def run_ours(args, rank, world, local_rank):
         roofline["traffic_source"] = "--traffic (DRAM bytes per launch from an ncu capture)"
     elif res == RES and args.de_kernel in (0, 2):
         roofline["traffic"] = DE_TRAFFIC_RES512
+        # pipe utilisation of the same launch in the same ncu capture
+        roofline["ncu_pipe_active"] = {"fma": 0.613, "alu": 0.252, "xu": 0.119,
+                                       "issue_slots": 0.901}
         roofline["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one "
                                       "k_de_grid_brick launch at res 512 (ncu --set full, "
                                       "profiles/k_de_grid_brick_res512.md)")
