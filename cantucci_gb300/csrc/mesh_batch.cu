@@ -8,11 +8,13 @@
 //
 //   step 1   one persistent kernel; warps take chunks of work items from an
 //            atomic queue.  An item is a 2x4x4 brick of corners (spans with
-//            res >= 32) or 32 consecutive corners in GridTable order (smaller
-//            spans, where bricks would leave lanes idle).
+//            res >= the batch's brick_min_res) or 32 consecutive corners in
+//            GridTable order (smaller spans, where bricks would leave lanes
+//            idle).
 //   step 2/3 grid-stride kernels over the cell rows of all spans; one
 //            exclusive scan over all rows gives every span's vertex range
-//            (and, for quads, its index range) in span order.
+//            (and, for quads, its index range) in span order.  The quads run
+//            on a side stream beside the vertex placement.
 // No launch depends on a host-side count, so a batch is captured into one
 // CUDA graph and replayed.
 //
