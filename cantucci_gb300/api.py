@@ -193,6 +193,13 @@ class MandelbulbPolar(Shape):
     def bounding_box(self) -> Span:
         return Span([-1.2, -1.2, -1.2], [1.2, 1.2, 1.2])
 
+    def fast(self) -> "MandelbulbPolar":
+        """Same shape with fast numerics: one branch-free arctangent instead
+        of acos and atan2, powers as exp2(P log2 r), SFU sin/cos."""
+        m = MandelbulbPolar(self.power, self.max_iters, self.bailout, self.rotation)
+        m.numerics = _ffi.CG_NUMERICS_FAST
+        return m
+
     def _cshape(self):
         s = _ffi.CgShape()
         s.kind = _ffi.CG_SHAPE_MANDELBULB_POLAR

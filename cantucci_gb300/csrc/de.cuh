@@ -515,6 +515,75 @@ __device__ __forceinline__ float mandelbulb_int_poly(int32_t P, uint32_t max_ite
     return x86_nan(0.5f * logf(r) * r / dr);
 }
 
+// ---- fast polar form (CG_NUMERICS_FAST) ----------------------------------
+//
+// The polar estimator with approximate transcendentals, for marching: one
+// branch-free arctangent instead of acosf and atan2f (theta = atan2(rho, z)
+// equals acos(z / r) for r = |(rho, z)|), powers as exp2(P log2 r), and sin /
+// cos after reduction to [-pi, pi] from the SFU.
+
+// atan(t), t in [0, 1]: t * p(t^2) with p of degree 7, fitted to atan(t)/t on
+// Chebyshev nodes by iteratively reweighted least squares (Lawson's
+// near-minimax method); |error| < 2e-7 when evaluated in f32.
+__device__ __forceinline__ float atan01(float t) {
+    const float u = t * t;
+    float p = -4.780781455e-03f;
+    p = fmaf(p, u, 2.455833741e-02f);
+    p = fmaf(p, u, -5.990651995e-02f);
+    p = fmaf(p, u, 9.942895174e-02f);
+    p = fmaf(p, u, -1.402947456e-01f);
+    p = fmaf(p, u, 1.997138709e-01f);
+    p = fmaf(p, u, -3.333209455e-01f);
+    p = fmaf(p, u, 9.999999404e-01f);
+    return t * p;
+}
+
+// atan2(y, x) by octant folding into atan01: selects, no branches.
+__device__ __forceinline__ float atan2_fast(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+    float r = atan01(mx > 0.0f ? __fdividef(mn, mx) : 0.0f);
+    r = ay > ax ? 1.57079633f - r : r;
+    r = x < 0.0f ? 3.14159265f - r : r;
+    return copysignf(r, y);
+}
+
+// sin and cos of x (|x| up to a few hundred): reduce by 2 pi, then the SFU.
+__device__ __forceinline__ void sincos_fast(float x, float* sn, float* cs) {
+    const float k = rintf(x * 0.159154943f);
+    __sincosf(fmaf(-k, 6.28318531f, x), sn, cs);
+}
+
+// One iteration of the polar loop (polar_step's contract, fast numerics).
+__device__ __forceinline__ bool polar_step_fast(float P, float bailout, float qx, float qy, float qz,
+                                                float& x, float& y, float& z, float& dr, float& r) {
+    const float rho2 = fmaf(x, x, y * y);
+    r = sqrtf(fmaf(z, z, rho2));
+    if (r > bailout) return false;
+    const float theta = atan2_fast(sqrtf(rho2), z) * P;
+    const float phi = atan2_fast(y, x) * P;
+    const float lr = __log2f(r);
+    const float zr = exp2f(P * lr);
+    dr = fmaf(exp2f((P - 1.0f) * lr) * P, dr, 1.0f);
+    float sn, cs, sp, cp;
+    sincos_fast(theta, &sn, &cs);
+    sincos_fast(phi, &sp, &cp);
+    x = fmaf(zr, sn * cp, qx);
+    y = fmaf(zr, sp * sn, qy);
+    z = fmaf(zr, cs, qz);
+    return true;
+}
+
+__device__ __forceinline__ float polar_de_fast(const ShapeDev& s, float px, float py, float pz) {
+    const float qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
+    const float qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
+    const float qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
+    float x = qx, y = qy, z = qz, dr = 1.0f, r = 0.0f;
+    for (uint32_t i = 0; i < s.max_iters; ++i)
+        if (!polar_step_fast(s.power_f, s.bailout, qx, qy, qz, x, y, z, dr, r)) break;
+    return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
+}
+
 // Kernel modes.
 enum Mode {
     MODE_P8 = 0,
@@ -522,7 +591,8 @@ enum Mode {
     MODE_POLAR = 2,
     MODE_SPHERE = 3,
     MODE_P8_FAST = 4,
-    MODE_INT_POLY = 5
+    MODE_INT_POLY = 5,
+    MODE_POLAR_FAST = 6
 };
 
 template <int M>
@@ -532,6 +602,7 @@ __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float
     if (M == MODE_POLAR) return polar_de(s, x, y, z);
     if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
     if (M == MODE_INT_POLY) return mandelbulb_int_poly(s.power, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_POLAR_FAST) return polar_de_fast(s, x, y, z);
     return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
 }
 
@@ -539,7 +610,8 @@ __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float
 // Kernel mode of a shape (integer P=8 takes the polynomial).
 __host__ __device__ __forceinline__ int mode_of(const ShapeDev& s, uint32_t numerics) {
     if (s.kind == CG_SHAPE_SPHERE) return MODE_SPHERE;
-    if (s.kind == CG_SHAPE_MANDELBULB_POLAR) return MODE_POLAR;
+    if (s.kind == CG_SHAPE_MANDELBULB_POLAR)
+        return numerics == CG_NUMERICS_FAST ? MODE_POLAR_FAST : MODE_POLAR;
     if (s.power == 8) return numerics == CG_NUMERICS_FAST ? MODE_P8_FAST : MODE_P8;
     return numerics == CG_NUMERICS_FAST && s.power >= 1 ? MODE_INT_POLY : MODE_INT;
 }

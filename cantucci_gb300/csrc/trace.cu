@@ -64,8 +64,9 @@ __global__ void __launch_bounds__(128) k_trace(ShapeDev s, CameraDev c, uint32_t
 }
 
 // The polar estimator one loop iteration at a time (the same operations as
-// polar_de), so that a lane can start a new estimate while its warp
-// neighbours are still iterating theirs.
+// polar_de, or polar_de_fast with FAST), so that a lane can start a new
+// estimate while its warp neighbours are still iterating theirs.
+template <bool FAST>
 struct PolarIter {
     float qx, qy, qz;  // R^T p
     StepState st;      // z, dr
@@ -73,9 +74,15 @@ struct PolarIter {
     uint32_t it;
 
     __device__ __forceinline__ void start(const ShapeDev& s, float px, float py, float pz) {
-        qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-        qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-        qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+        if (FAST) {
+            qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
+            qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
+            qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
+        } else {
+            qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+            qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+            qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+        }
         st = {qx, qy, qz, 1.0f};
         r = 0.0f;
         it = 0;
@@ -84,14 +91,15 @@ struct PolarIter {
     // last iteration ran: r is then the stale |z| of that iteration).
     __device__ __forceinline__ bool advance(const ShapeDev& s) {
         float ri;
-        if (!polar_step(s, qx, qy, qz, st, ri)) {
-            r = ri;
-            return true;
-        }
+        const bool go = FAST ? polar_step_fast(s.power_f, s.bailout, qx, qy, qz, st.x, st.y,
+                                               st.z, st.dr, ri)
+                             : polar_step(s, qx, qy, qz, st, ri);
         r = ri;
+        if (!go) return true;
         return ++it >= s.max_iters;
     }
     __device__ __forceinline__ float value() const {
+        if (FAST) return x86_nan(__fdividef(0.5f * __logf(r) * r, st.dr));
         const float ln_r = __fmul_rn(logf(r), r);
         return x86_nan(__fdiv_rn(__fmul_rn(0.5f, ln_r), st.dr));
     }
@@ -113,7 +121,8 @@ __global__ void __launch_bounds__(128) k_trace_queue(ShapeDev s, CameraDev c, ui
     uint32_t i = kNone, k = 0;
     bool done = false;
     float d[3] = {0.0f, 0.0f, 0.0f}, t = 0.0f;
-    PolarIter pe;
+    constexpr bool kIter = M == MODE_POLAR || M == MODE_POLAR_FAST;
+    PolarIter<M == MODE_POLAR_FAST> pe;
     for (;;) {
         const bool need = !done && i == kNone;
         const unsigned need_mask = __ballot_sync(0xFFFFFFFFu, need);
@@ -133,14 +142,14 @@ __global__ void __launch_bounds__(128) k_trace_queue(ShapeDev s, CameraDev c, ui
                     pixel_ray(c, i, d);
                     t = 0.0f;
                     k = 0;
-                    if (M == MODE_POLAR) pe.start(s, c.eye[0], c.eye[1], c.eye[2]);
+                    if (kIter) pe.start(s, c.eye[0], c.eye[1], c.eye[2]);
                 }
             }
         }
         if (__all_sync(0xFFFFFFFFu, done)) break;
         if (done || i == kNone) continue;
         float de;
-        if (M == MODE_POLAR) {
+        if (kIter) {
             if (!pe.advance(s)) continue;
             de = pe.value();
         } else {
@@ -160,7 +169,7 @@ __global__ void __launch_bounds__(128) k_trace_queue(ShapeDev s, CameraDev c, ui
         if (fin) {
             depth[i] = out;
             i = kNone;
-        } else if (M == MODE_POLAR) {
+        } else if (kIter) {
             pe.start(s, c.eye[0] + t * d[0], c.eye[1] + t * d[1], c.eye[2] + t * d[2]);
         }
     }
@@ -260,7 +269,7 @@ using namespace cg;
 extern "C" {
 
 cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_t max_steps,
-                         float eps_scale, float* depth, void* stream) {
+                         float eps_scale, uint32_t numerics, float* depth, void* stream) {
     if (!shape || !depth) {
         set_error("NULL argument");
         return CG_EINVAL;
@@ -272,10 +281,19 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     cudaStream_t st = (cudaStream_t)stream;
     if (g_trace_kernel == 0) {
         const unsigned G = grid_for(n, 128, 16);
-        switch (mode_of(s, CG_NUMERICS_EXACT)) {
+        switch (mode_of(s, numerics)) {
         case MODE_P8: k_trace<MODE_P8><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
         case MODE_INT: k_trace<MODE_INT><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
         case MODE_POLAR: k_trace<MODE_POLAR><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
+        case MODE_POLAR_FAST:
+            k_trace<MODE_POLAR_FAST><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth);
+            break;
+        case MODE_P8_FAST:
+            k_trace<MODE_P8_FAST><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth);
+            break;
+        case MODE_INT_POLY:
+            k_trace<MODE_INT_POLY><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth);
+            break;
         default: k_trace<MODE_SPHERE><<<G, 128, 0, st>>>(s, c, max_steps, eps_scale, depth); break;
         }
         CG_CHECK_LAUNCH("k_trace");
@@ -284,10 +302,19 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     uint32_t* next = nullptr;
     CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&next), sizeof(uint32_t), st));
     CG_CUDA(cudaMemsetAsync(next, 0, sizeof(uint32_t), st));
-    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    switch (mode_of(s, numerics)) {
     case MODE_P8: launch_trace_queue<MODE_P8>(s, c, max_steps, eps_scale, depth, next, st); break;
     case MODE_INT: launch_trace_queue<MODE_INT>(s, c, max_steps, eps_scale, depth, next, st); break;
     case MODE_POLAR: launch_trace_queue<MODE_POLAR>(s, c, max_steps, eps_scale, depth, next, st); break;
+    case MODE_POLAR_FAST:
+        launch_trace_queue<MODE_POLAR_FAST>(s, c, max_steps, eps_scale, depth, next, st);
+        break;
+    case MODE_P8_FAST:
+        launch_trace_queue<MODE_P8_FAST>(s, c, max_steps, eps_scale, depth, next, st);
+        break;
+    case MODE_INT_POLY:
+        launch_trace_queue<MODE_INT_POLY>(s, c, max_steps, eps_scale, depth, next, st);
+        break;
     default: launch_trace_queue<MODE_SPHERE>(s, c, max_steps, eps_scale, depth, next, st); break;
     }
     const cudaError_t le = cudaGetLastError();

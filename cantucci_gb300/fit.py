@@ -49,13 +49,16 @@ def _shape(power, rot, max_iters, bailout):
 
 
 def render(power, rot, cam, max_steps=256, eps_scale=1e-4, max_iters=15, bailout=2.5,
-           out=None):
-    """(height, width) CUDA depth map; -1 where the ray misses."""
+           out=None, fast=False):
+    """(height, width) CUDA depth map; -1 where the ray misses.  fast=True
+    marches with the fast polar estimator (branch-free arctangent, SFU
+    powers and sin/cos): same hits to within the march's tolerance."""
     torch = _torch()
     if out is None:
         out = torch.empty((cam.height, cam.width), dtype=torch.float32, device="cuda")
     shape = _shape(power, rot, max_iters, bailout)
-    check(load().cg_trace_depth(C.byref(shape), C.byref(cam), max_steps, eps_scale,
+    numerics = _ffi.CG_NUMERICS_FAST if fast else _ffi.CG_NUMERICS_EXACT
+    check(load().cg_trace_depth(C.byref(shape), C.byref(cam), max_steps, eps_scale, numerics,
                                 C.c_void_p(out.data_ptr()),
                                 C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return out
@@ -66,13 +69,15 @@ def _make_render_fn():
 
     class DepthRender(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, power, rot, cam, max_steps, eps_scale, max_iters, bailout):
+        def forward(ctx, power, rot, cam, max_steps, eps_scale, max_iters, bailout, fast):
             p = float(power)
             r = [float(v) for v in rot.detach().cpu()]
-            depth = render(p, r, cam, max_steps, eps_scale, max_iters, bailout)
+            depth = render(p, r, cam, max_steps, eps_scale, max_iters, bailout, fast=fast)
             ctx.save_for_backward(depth)
             ctx.shape = _shape(p, r, max_iters, bailout)
             ctx.cam = cam
+            ctx.param_devices = (power.device if torch.is_tensor(power) else None,
+                                 rot.device if torch.is_tensor(rot) else None)
             return depth
 
         @staticmethod
@@ -84,7 +89,9 @@ def _make_render_fn():
                                            C.c_void_p(depth.data_ptr()), C.c_void_p(g.data_ptr()),
                                            C.c_void_p(params.data_ptr()),
                                            C.c_void_p(torch.cuda.current_stream().cuda_stream)))
-            return params[0].cpu(), params[1:4].cpu(), None, None, None, None, None
+            pdev, rdev = ctx.param_devices
+            return (params[0].to(pdev), params[1:4].to(rdev), None, None, None, None, None,
+                    None)
 
     return DepthRender
 
@@ -92,11 +99,12 @@ def _make_render_fn():
 _RENDER = None
 
 
-def depth_render(power, rot, cam, max_steps=256, eps_scale=1e-4, max_iters=15, bailout=2.5):
+def depth_render(power, rot, cam, max_steps=256, eps_scale=1e-4, max_iters=15, bailout=2.5,
+                 fast=False):
     global _RENDER
     if _RENDER is None:
         _RENDER = _make_render_fn()
-    return _RENDER.apply(power, rot, cam, max_steps, eps_scale, max_iters, bailout)
+    return _RENDER.apply(power, rot, cam, max_steps, eps_scale, max_iters, bailout, fast)
 
 
 def l1_loss(depth, target):
@@ -107,8 +115,9 @@ def l1_loss(depth, target):
 
 
 def fit(target, cam, power0=8.0, rot0=(0.0, 0.0, 0.0), steps=300, lr=1e-2, max_steps=256,
-        eps_scale=1e-4, callback=None):
-    """Adam on (power, rotation); returns (power, rot, losses)."""
+        eps_scale=1e-4, callback=None, fast=False):
+    """Adam on (power, rotation); returns (power, rot, losses).  fast=True
+    marches with the fast estimator; the gradient is exact either way."""
     torch = _torch()
     power = torch.tensor(float(power0), requires_grad=True)
     rot = torch.tensor([float(v) for v in rot0], requires_grad=True)
@@ -116,7 +125,7 @@ def fit(target, cam, power0=8.0, rot0=(0.0, 0.0, 0.0), steps=300, lr=1e-2, max_s
     losses = []
     for it in range(steps):
         opt.zero_grad()
-        depth = depth_render(power, rot, cam, max_steps, eps_scale)
+        depth = depth_render(power, rot, cam, max_steps, eps_scale, fast=fast)
         loss = l1_loss(depth, target)
         loss.backward()
         opt.step()

@@ -51,7 +51,8 @@ enum {
     CG_NUMERICS_EXACT = 0,  /* IEEE f32, reference operation order: bit-identical loop state */
     CG_NUMERICS_FAST = 1    /* not bit-faithful: P=8 FMA-contracted with approximate div/sqrt;
                                other integer powers trig-free (complex powers, no acos/atan2/
-                               sin/cos) */
+                               sin/cos); the polar form with a branch-free arctangent, SFU
+                               powers and sin/cos */
 };
 
 /* Normals of the mesher. */
@@ -395,10 +396,12 @@ typedef struct cg_camera {
 
 /* Depth map by sphere tracing every pixel's ray: the march of
  * ShapeMesh::get_focii (src/mesh/mod.rs:229-241) per pixel, hit when
- * DE < eps_scale * t * (pixel angle), at most max_steps steps.
+ * DE < eps_scale * t * (pixel angle), at most max_steps steps.  numerics:
+ * CG_NUMERICS_EXACT, or CG_NUMERICS_FAST (for the polar form: one branch-free
+ * arctangent, SFU powers and sin/cos).
  * depth: device, width*height floats, ray distance t or -1 for a miss. */
 cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_t max_steps,
-                         float eps_scale, float* depth, void* stream);
+                         float eps_scale, uint32_t numerics, float* depth, void* stream);
 
 /* Implicit-surface backward of cg_trace_depth for the polar shape: at a hit
  * x = eye + t d, DE(x; theta) = 0 gives dt/dtheta = -(dDE/dtheta) /

@@ -155,10 +155,39 @@ def test_queue_march_matches_per_pixel_march(cg, kind):
             _ffi.check(lib.cg_set_option(b"trace_kernel", k))
             d = torch.empty((cam.height, cam.width), dtype=torch.float32, device="cuda")
             _ffi.check(lib.cg_trace_depth(C.byref(shape._cshape()), C.byref(cam), 256, 1e-4,
-                                          C.c_void_p(d.data_ptr()), None))
+                                          0, C.c_void_p(d.data_ptr()), None))
             torch.cuda.synchronize()
             outs.append(d.cpu().numpy())
     finally:
         lib.cg_set_option(b"trace_kernel", 1)
     assert (outs[0] > 0).sum() > 1000
     assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
+def test_fast_march_close_to_exact(cg, orc):
+    """The fast polar estimator (branch-free arctangent, SFU powers and
+    sin/cos) marches to the same hits: depths agree with the exact march to
+    well under the march's own tolerance, and its DE tracks FP64."""
+    import torch
+    from cantucci_gb300 import fit
+    cam = fit.camera(128, 128)
+    rot = (0.2, 0.1, 0.0)
+    a = fit.render(8.3, rot, cam).cpu().numpy()
+    b = fit.render(8.3, rot, cam, fast=True).cpu().numpy()
+    assert np.mean((a > 0) == (b > 0)) > 0.995
+    both = (a > 0) & (b > 0)
+    err = np.abs(a[both] - b[both])
+    assert np.median(err) < 1e-5 and np.mean(err < 1e-3) > 0.99, np.quantile(err, [0.5, 0.99])
+    # the estimator itself against FP64 on random points
+    pts = W_uniform(100_000)
+    s = cg.MandelbulbPolar(8.3, 15, 2.5, rot)
+    d = s.fast().batch_min_distance_from(pts).astype(np.float64)
+    ref = orc.de_f64(orc.mandelbulb_polar(8.3, 15, 2.5, rot), pts)
+    ok = np.isfinite(ref)
+    close = np.abs(d[ok] - ref[ok]) <= 1e-5 + 1e-3 * np.abs(ref[ok])
+    assert close.mean() >= 0.99, close.mean()
+
+
+def W_uniform(n):
+    from cantucci_gb300 import workloads as W
+    return W.uniform_points(n, seed=41)
