@@ -396,6 +396,7 @@ def extra_de_variants(dev, res=RES):
     p6 = cg.Mandelbulb(6, 15, 2.5)
     for name, shape in (("exact_p8", exact), ("fast_p8", exact.fast()),
                         ("polar_p8.0", cg.MandelbulbPolar(8.0, 15, 2.5)),
+                        ("polar_p8.0_fast", cg.MandelbulbPolar(8.0, 15, 2.5).fast()),
                         ("trig_p6", p6), ("trig_free_p6", p6.fast())):
         ms = _time_cuda(lambda: shape.span_grid(span, res, out=out), reps=5, warm=2)
         e = {"ms": ms, "pts_per_s": n ** 3 / (ms * 1e-3)}
