@@ -292,6 +292,8 @@ def extra_normals(dev, n=16 << 20, cpu=True):
     ms_adj = _time_cuda(lambda: de_grad(pts, 8.0), reps=2)
     ms_tan = _time_cuda(lambda: de_grad(pts, 8.0, mode="tangent", with_power=False), reps=2)
     ms_tan4 = _time_cuda(lambda: de_grad(pts, 8.0, mode="tangent"), reps=2)
+    ms_tanf = _time_cuda(lambda: de_grad(pts, 8.0, mode="tangent", with_power=False, fast=True),
+                         reps=2)
     ms_fd = _time_cuda(lambda: fd_grad(pts, shape, 1e-4), reps=2)
     out = {"workload": "%d points in |DE| < 1e-3 (uniform in [-1.2,1.2]^3, 8 sphere-trace steps "
                        "along random directions), polar Mandelbulb power 8, max_iters 15" % n,
@@ -303,6 +305,8 @@ def extra_normals(dev, n=16 << 20, cpu=True):
            "adjoint_vs_fd6_speedup": ms_fd / ms_adj,
            "tangent_normals_vs_fd6_speedup": ms_fd / ms_tan,
            "tangent_all_vs_fd6_speedup": ms_fd / ms_tan4,
+           "fwd_tangent_fast_normals_pts_per_s": n / (ms_tanf * 1e-3),
+           "tangent_fast_normals_vs_fd6_speedup": ms_fd / ms_tanf,
            "modes": "adjoint = reverse mode with checkpoint recompute (DE, grad, d/dpower, "
                     "d/drotation); tangent_normals = forward mode along x, y, z (DE, grad, "
                     "d/drotation); tangent_all = forward mode with the power direction too"}
@@ -314,6 +318,8 @@ def extra_normals(dev, n=16 << 20, cpu=True):
         ref = oracle.de_grad_f64(oracle.mandelbulb_polar(8.0, 15, 2.5), sub.cpu().numpy())
         a = de_grad(sub, 8.0).cpu().numpy().astype(np.float64)
         t = de_grad(sub, 8.0, mode="tangent", with_power=False).cpu().numpy().astype(np.float64)
+        tf = de_grad(sub, 8.0, mode="tangent", with_power=False,
+                     fast=True).cpu().numpy().astype(np.float64)
         f = fd_grad(sub, shape, 1e-4).cpu().numpy().astype(np.float64)
 
         def ang(x, y):
@@ -327,6 +333,7 @@ def extra_normals(dev, n=16 << 20, cpu=True):
         out["angle_deg_vs_fp64"] = {
             "adjoint": stats(ang(a[ok, 1:4], ref[ok, 1:4])),
             "tangent": stats(ang(t[ok, 1:4], ref[ok, 1:4])),
+            "tangent_fast": stats(ang(tf[ok, 1:4], ref[ok, 1:4])),
             "fd6_h1e-4": stats(ang(f[ok], ref[ok, 1:4]))}
         # no step size brings the f32 central difference to the adjoint's error
         for h in (1e-2, 1e-3, 3e-4, 3e-5, 1e-5):

@@ -87,13 +87,17 @@ def mandelbulb_de(points, power, rot, max_iters: int = 15, bailout: float = 2.5)
 
 
 def de_grad(points, power: float, rot=(0.0, 0.0, 0.0), max_iters: int = 15,
-            bailout: float = 2.5, mode: str = "adjoint", with_power: bool = True):
+            bailout: float = 2.5, mode: str = "adjoint", with_power: bool = True,
+            fast: bool = False):
     """(n, 8) CUDA tensor: DE, dDE/dp (3), dDE/dpower, dDE/d(euler) (3).
 
     mode "adjoint": reverse mode with checkpoint recompute (cg_de_grad).
     mode "tangent": forward mode, one pass (cg_de_grad_tangent); with
     with_power=False it skips the power direction (column 4 is 0), which is
-    all a normal needs."""
+    all a normal needs; fast=True iterates with the fast polar estimator's
+    arithmetic."""
+    if fast and mode != "tangent":
+        raise ValueError("fast numerics are for mode 'tangent'")
     torch = _torch()
     pts = points.contiguous().float()
     out = torch.empty((pts.shape[0], 8), dtype=torch.float32, device=pts.device)
@@ -103,9 +107,9 @@ def de_grad(points, power: float, rot=(0.0, 0.0, 0.0), max_iters: int = 15,
         check(load().cg_de_grad(C.byref(shape), C.c_void_p(pts.data_ptr()), pts.shape[0],
                                 C.c_void_p(out.data_ptr()), stream))
     elif mode == "tangent":
+        flags = (1 if with_power else 0) | (2 if fast else 0)
         check(load().cg_de_grad_tangent(C.byref(shape), C.c_void_p(pts.data_ptr()),
-                                        pts.shape[0], int(bool(with_power)),
-                                        C.c_void_p(out.data_ptr()), stream))
+                                        pts.shape[0], flags, C.c_void_p(out.data_ptr()), stream))
     else:
         raise ValueError("mode is 'adjoint' or 'tangent'")
     return out

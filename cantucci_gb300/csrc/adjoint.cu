@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(128) k_de_grad(ShapeDev s, Dm3 dm, const float
     }
 }
 
-template <int T>
+template <int T, bool FAST>
 __global__ void __launch_bounds__(128) k_de_grad_tangent(ShapeDev s, Dm3 dm,
                                                          const float* __restrict__ pts, uint64_t n,
                                                          float* __restrict__ out) {
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(128) k_de_grad_tangent(ShapeDev s, Dm3 dm,
         float x = 0.0f, y = 0.0f, z = 0.0f;
         if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
         float o[8];
-        polar_de_tangent<T>(s, dm.m, x, y, z, o);
+        polar_de_tangent<T, true, FAST>(s, dm.m, x, y, z, o);
         store8(out, base + (threadIdx.x & 31), o);
     }
 }
@@ -165,7 +165,7 @@ cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, flo
 }
 
 cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
-                             uint32_t with_power, float* out, void* stream) {
+                             uint32_t flags, float* out, void* stream) {
     if (!shape || shape->kind != CG_SHAPE_MANDELBULB_POLAR || shape->max_iters < 1) {
         set_error("the gradient is defined on the real-power polar Mandelbulb (kind 2)");
         return CG_EINVAL;
@@ -177,12 +177,18 @@ cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_
     if (!n) return CG_OK;
     const unsigned G = grid_for(n, 128, 16);
     cudaStream_t st = (cudaStream_t)stream;
-    if (with_power)
-        k_de_grad_tangent<4><<<G, 128, 0, st>>>(make_shape_dev(*shape),
-                                                rotation_derivatives(*shape), points, n, out);
-    else
-        k_de_grad_tangent<3><<<G, 128, 0, st>>>(make_shape_dev(*shape),
-                                                rotation_derivatives(*shape), points, n, out);
+    if (flags & ~3u) {
+        set_error("cg_de_grad_tangent flags: CG_GRAD_POWER | CG_GRAD_FAST");
+        return CG_EINVAL;
+    }
+    const ShapeDev sd = make_shape_dev(*shape);
+    const Dm3 dm = rotation_derivatives(*shape);
+    switch (flags) {
+    case 0: k_de_grad_tangent<3, false><<<G, 128, 0, st>>>(sd, dm, points, n, out); break;
+    case CG_GRAD_POWER: k_de_grad_tangent<4, false><<<G, 128, 0, st>>>(sd, dm, points, n, out); break;
+    case CG_GRAD_FAST: k_de_grad_tangent<3, true><<<G, 128, 0, st>>>(sd, dm, points, n, out); break;
+    default: k_de_grad_tangent<4, true><<<G, 128, 0, st>>>(sd, dm, points, n, out); break;
+    }
     CG_CHECK_LAUNCH("k_de_grad_tangent");
     return CG_OK;
 }

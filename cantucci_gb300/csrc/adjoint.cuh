@@ -222,12 +222,19 @@ __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __
 // the three point directions).  Work: one forward pass plus T tangent
 // updates of ~30 operations per step, against polar_de_grad's two forward
 // passes plus one backward step.
-template <int T, bool Rot = true>
+template <int T, bool Rot = true, bool FAST = false>
 __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float* __restrict__ dm,
                                                  float px, float py, float pz, float* out) {
-    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-    const float qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    float qx, qy, qz;
+    if (FAST) {
+        qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
+        qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
+        qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
+    } else {
+        qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+        qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+        qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    }
     const float P = s.power_f;
     float zx = qx, zy = qy, zz = qz, dr = 1.0f, r = 0.0f;
     // tangents: direction k has (tx, ty, tz, tdr); dq_k = e_k for k < 3
@@ -241,23 +248,34 @@ __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float*
         tr[k] = 0.0f;
     }
     for (uint32_t i = 0; i < s.max_iters; ++i) {
-        r = magnitude<Exact>(zx, zy, zz);
+        const float rho2 = zx * zx + zy * zy;
+        r = FAST ? sqrtf(fmaf(zz, zz, rho2)) : magnitude<Exact>(zx, zy, zz);
         const float inv_r = 1.0f / r;
 #pragma unroll
         for (int k = 0; k < T; ++k) tr[k] = (zx * tx[k] + zy * ty[k] + zz * tz[k]) * inv_r;
         if (r > s.bailout) break;
-        const float theta = acosf(__fdiv_rn(zz, r));
-        const float phi = atan2f(zy, zx);
-        const float t1 = powf(r, __fsub_rn(P, 1.0f));
-        const float dr_old = dr;
-        dr = __fadd_rn(__fmul_rn(__fmul_rn(t1, P), dr), 1.0f);
-        const float zr = powf(r, P);
-        float sn, cs, sp, cp;
-        sincosf(__fmul_rn(theta, P), &sn, &cs);
-        sincosf(__fmul_rn(phi, P), &sp, &cp);
-        // shared factors of the tangent step
-        const float rho2 = zx * zx + zy * zy;
         const float rho = sqrtf(rho2);
+        float theta, phi, t1, zr, sn, cs, sp, cp;
+        const float dr_old = dr;
+        if (FAST) {  // polar_step_fast's arithmetic
+            theta = atan2_fast(rho, zz);
+            phi = atan2_fast(zy, zx);
+            const float lr = __log2f(r);
+            zr = exp2f(P * lr);
+            t1 = exp2f((P - 1.0f) * lr);
+            dr = fmaf(t1 * P, dr, 1.0f);
+            sincos_fast(theta * P, &sn, &cs);
+            sincos_fast(phi * P, &sp, &cp);
+        } else {
+            theta = acosf(__fdiv_rn(zz, r));
+            phi = atan2f(zy, zx);
+            t1 = powf(r, __fsub_rn(P, 1.0f));
+            dr = __fadd_rn(__fmul_rn(__fmul_rn(t1, P), dr), 1.0f);
+            zr = powf(r, P);
+            sincosf(__fmul_rn(theta, P), &sn, &cs);
+            sincosf(__fmul_rn(phi, P), &sp, &cp);
+        }
+        // shared factors of the tangent step
         const bool off_axis = rho > 1e-30f;
         const float inv_rho = off_axis ? 1.0f / rho : 0.0f;
         const float inv_rho2 = off_axis ? 1.0f / rho2 : 0.0f;
@@ -269,7 +287,7 @@ __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float*
         const float ax = zr * cs * cp, ay = zr * sp * cs, az = -zr * sn;  // zr du/dTh
         const float bx = -zr * sn * sp, by = zr * cp * sn;                // zr du/dPh
         float lnr = 0.0f;
-        if (T == 4) lnr = logf(r);
+        if (T == 4) lnr = FAST ? __logf(r) : logf(r);
 #pragma unroll
         for (int k = 0; k < T; ++k) {
             const float th_t = (zz * (zx * tx[k] + zy * ty[k]) * inv_rho - rho * tz[k]) * inv_r2;
@@ -288,14 +306,21 @@ __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float*
             tz[k] = zr_t * uz + Th_t * az + (k == 2 ? 1.0f : 0.0f);
             tdr[k] = dr_t;
         }
-        zx = __fadd_rn(__fmul_rn(zr, __fmul_rn(sn, cp)), qx);
-        zy = __fadd_rn(__fmul_rn(zr, __fmul_rn(sp, sn)), qy);
-        zz = __fadd_rn(__fmul_rn(zr, cs), qz);
+        if (FAST) {
+            zx = fmaf(zr, sn * cp, qx);
+            zy = fmaf(zr, sp * sn, qy);
+            zz = fmaf(zr, cs, qz);
+        } else {
+            zx = __fadd_rn(__fmul_rn(zr, __fmul_rn(sn, cp)), qx);
+            zy = __fadd_rn(__fmul_rn(zr, __fmul_rn(sp, sn)), qy);
+            zz = __fadd_rn(__fmul_rn(zr, cs), qz);
+        }
     }
     // tr holds r' of the returned r: the escaping iterate's, or the stale
     // one of the last step when the loop runs out (tdr is then dr_N's).
-    const float ln_r = logf(r);
-    const float de = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(ln_r, r)), dr);
+    const float ln_r = FAST ? __logf(r) : logf(r);
+    const float de = FAST ? __fdividef(0.5f * ln_r * r, dr)
+                          : __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(ln_r, r)), dr);
     const float c_r = 0.5f * (ln_r + 1.0f) / dr, c_dr = -de / dr;
     float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll

@@ -424,12 +424,14 @@ cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, flo
                      void* stream);
 
 /* The same derivatives in forward (tangent) mode: one pass carries d/dq
- * along x, y, z (and, with with_power != 0, d/dpower) next to the iterate,
- * so there is no recompute.  Same out layout as cg_de_grad; with
- * with_power == 0, out[4] (dDE/dpower) is 0 and the rest is computed.  Any
- * max_iters >= 1.  No reference counterpart. */
+ * along x, y, z (and, with CG_GRAD_POWER in flags, d/dpower) next to the
+ * iterate, so there is no recompute.  Same out layout as cg_de_grad; without
+ * CG_GRAD_POWER, out[4] (dDE/dpower) is 0 and the rest is computed.  With
+ * CG_GRAD_FAST the iteration uses the fast polar estimator's arithmetic
+ * (CG_NUMERICS_FAST).  Any max_iters >= 1.  No reference counterpart. */
+enum { CG_GRAD_POWER = 1, CG_GRAD_FAST = 2 };
 cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
-                             uint32_t with_power, float* out, void* stream);
+                             uint32_t flags, float* out, void* stream);
 
 /* Backward of DE over a batch (the autograd.Function backward): given the
  * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to

@@ -223,3 +223,27 @@ def test_tangent_mode_any_max_iters(cg, orc):
     g = de_grad(p, 8.0, max_iters=80, mode="tangent").cpu().numpy().astype(np.float64)
     d = cg.MandelbulbPolar(8.0, 80, 2.5).batch_min_distance_from(p).cpu().numpy()
     np.testing.assert_array_equal(d.view(np.uint32), g[:, 0].astype(np.float32).view(np.uint32))
+
+
+def test_tangent_fast_numerics(cg, orc):
+    """Forward mode with the fast polar arithmetic: normals close to the
+    exact forward mode away from the surface, and in the band most of them
+    still within 0.1 degree of FP64."""
+    import torch
+    from cantucci_gb300.autograd import de_grad
+    shape = cg.MandelbulbPolar(8.0, 15, 2.5)
+    p = torch.as_tensor(W.uniform_points(200_000, seed=24)).cuda()
+    d = shape.batch_min_distance_from(p)
+    far = p[(d > 0.02) & (d < 0.3)][:3000].contiguous()
+    a = de_grad(far, 8.0, mode="tangent", with_power=False).cpu().numpy()
+    b = de_grad(far, 8.0, mode="tangent", with_power=False, fast=True).cpu().numpy()
+    ang = angle_deg(b[:, 1:4].astype(np.float64), a[:, 1:4].astype(np.float64))
+    assert np.mean(ang < 0.01) >= 0.99, np.quantile(ang, [0.5, 0.99])
+    band = band_points(cg, 2000, 8.0, seed=25)
+    g = de_grad(band, 8.0, mode="tangent", with_power=False, fast=True).cpu().numpy()
+    ref = orc.de_grad_f64(orc.mandelbulb_polar(8.0, 15, 2.5), band.cpu().numpy())
+    ok = np.all(np.isfinite(ref[:, 1:4]), axis=1) & np.all(np.isfinite(g[:, 1:4]), axis=1)
+    ang64 = angle_deg(g[ok, 1:4].astype(np.float64), ref[ok, 1:4])
+    assert np.mean(ang64 < 0.1) >= 0.8, np.mean(ang64 < 0.1)
+    with pytest.raises(ValueError):
+        de_grad(band, 8.0, fast=True)
