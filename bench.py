@@ -617,6 +617,46 @@ def extra_root_crossings(dev, res=RES):
     return out
 
 
+def extra_dual_contouring(dev, res=RES):
+    """The 513^3 span with the reference's centroid placement and with the
+    dual-contouring vertex (one forward-mode gradient per crossing, a 3x3
+    QEF per cell), with linear and with root-found (4 Illinois steps)
+    crossings: mesh time and the median |DE| at the vertices."""
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    span = cg.Span(*W.SPAN_C1)
+    shape = cg.Mandelbulb(**SHAPE)
+    vcap, icap = res ** 3 // 16, 18 * res ** 3 // 16
+    v = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(icap, dtype=torch.int32, device=dev)
+    out = {"workload": "Mandelbulb P=8 max_iters 15, %d^3 corners" % (res + 1)}
+    m = cg.Mesher(dev)
+    try:
+        for name, placement, crossings in (("centroid", "centroid", "lerp"),
+                                           ("qef", "qef", "lerp"),
+                                           ("qef_root", "qef", "root")):
+            m.set_placement(placement)
+            m.set_crossings(crossings, 4)
+            m.generate_device(span, shape, res, v, i, strict=False)
+            best, best2 = None, None
+            for _ in range(3):
+                nv, ni, tm = m.generate_device(span, shape, res, v, i, strict=False)
+                ms = tm.first_ms + tm.second_ms + tm.third_ms
+                if best is None or ms < best:
+                    best, best2 = ms, tm.second_ms
+            de = v[:nv, 6].abs()
+            de = de[torch.isfinite(de)]
+            out[name] = {"mesh_ms": best, "step2_ms": best2, "vertices": nv,
+                         "median_abs_de_at_vertex": float(de.median())}
+    finally:
+        m.close()
+    for name in ("qef", "qef_root"):
+        out[name]["de_ratio"] = (out[name]["median_abs_de_at_vertex"]
+                                 / out["centroid"]["median_abs_de_at_vertex"])
+    return out
+
+
 def run_extras(args, dev):
     """The other configurations.  The oracle runs only in CPU legs (the CPU
     builder's timing and the accuracy checks against FP64), which
@@ -629,6 +669,7 @@ def run_extras(args, dev):
             ("normals", lambda: extra_normals(dev, cpu=cpu)),
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
             ("root_crossings", lambda: extra_root_crossings(dev)),
+            ("dual_contouring", lambda: extra_dual_contouring(dev)),
             ("lod", lambda: extra_lod(dev, cpu)),
             ("depth_fit", lambda: extra_depth_fit(dev, args.fit_steps))]
     if cpu:

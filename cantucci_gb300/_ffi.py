@@ -19,6 +19,7 @@ CG_SHAPE_MANDELBULB, CG_SHAPE_SPHERE, CG_SHAPE_MANDELBULB_POLAR = 0, 1, 2
 CG_NUMERICS_EXACT, CG_NUMERICS_FAST = 0, 1
 CG_NORMALS_FD, CG_NORMALS_ADJOINT = 0, 1
 CG_CROSSINGS_LERP, CG_CROSSINGS_ROOT = 0, 1
+CG_PLACEMENT_CENTROID, CG_PLACEMENT_QEF = 0, 1
 
 
 class CgShape(C.Structure):
@@ -103,6 +104,7 @@ SIGNATURES = [
     ("cg_mesher_destroy", None, [_vp]),
     ("cg_mesher_set_normals", _i32, [_vp, _u32]),
     ("cg_mesher_set_crossings", _i32, [_vp, _u32, _u32]),
+    ("cg_mesher_set_placement", _i32, [_vp, _u32]),
     ("cg_generate_for_box", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
                                    C.POINTER(_u64), C.POINTER(_u64), _tmp]),
     ("cg_generate_for_box_device", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
@@ -131,6 +133,7 @@ SIGNATURES = [
     ("cg_trace_backward", _i32, [_shp, C.c_void_p, _vp, _vp, _vp, _vp]),
     ("cg_de_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
     ("cg_de_grad_tangent", _i32, [_shp, _vp, _u64, _u32, _vp, _vp]),
+    ("cg_de_spatial_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
     ("cg_de_backward", _i32, [_shp, _vp, _vp, _u64, _vp, _vp, _vp]),
     ("cg_fd_grad", _i32, [_shp, _vp, _u64, _f32, _vp, _vp]),
     ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),

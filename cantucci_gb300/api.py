@@ -286,6 +286,14 @@ class Mesher:
         modes = {"lerp": _ffi.CG_CROSSINGS_LERP, "root": _ffi.CG_CROSSINGS_ROOT}
         check(self._lib.cg_mesher_set_crossings(self.handle, modes[mode], int(iters)))
 
+    def set_placement(self, mode: str):
+        """"centroid": the crossings' centroid, naive surface nets (default);
+        "qef": dual contouring -- the minimiser of the squared distances to
+        the tangent planes at the crossings, clamped to the cell (same cells
+        and indices)."""
+        modes = {"centroid": _ffi.CG_PLACEMENT_CENTROID, "qef": _ffi.CG_PLACEMENT_QEF}
+        check(self._lib.cg_mesher_set_placement(self.handle, modes[mode]))
+
     def generate(self, span: Span, shape: Shape, resolution: int, vertex_cap=None,
                  index_cap=None, vertices=None, indices=None, strict: bool = True):
         """Mesh into host numpy arrays (pinned torch tensors also accepted).

@@ -115,6 +115,18 @@ def de_grad(points, power: float, rot=(0.0, 0.0, 0.0), max_iters: int = 15,
     return out
 
 
+def spatial_grad(points, shape):
+    """(n, 4) CUDA tensor: DE and dDE/dp of any shape, one forward-mode pass
+    per point (cg_de_spatial_grad)."""
+    torch = _torch()
+    pts = points.contiguous().float()
+    out = torch.empty((pts.shape[0], 4), dtype=torch.float32, device=pts.device)
+    check(load().cg_de_spatial_grad(C.byref(shape._cshape()), C.c_void_p(pts.data_ptr()),
+                                    pts.shape[0], C.c_void_p(out.data_ptr()),
+                                    C.c_void_p(torch.cuda.current_stream(pts.device).cuda_stream)))
+    return out
+
+
 def fd_grad(points, shape, h: float):
     """(n, 3) central-difference gradient with six estimator calls per point."""
     torch = _torch()

@@ -8,6 +8,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "point_io.cuh"
+#include "qef.cuh"
 
 namespace cg {
 
@@ -48,6 +49,31 @@ __global__ void __launch_bounds__(128) k_de_grad_tangent(ShapeDev s, Dm3 dm,
         float o[8];
         polar_de_tangent<T, true, FAST>(s, dm.m, x, y, z, o);
         store8(out, base + (threadIdx.x & 31), o);
+    }
+}
+
+// DE and dDE/dp of any shape (shape_gradient), one 16-byte store per point
+// when `out` is 16-byte aligned.  The DE is the estimator's, bit for bit
+// (for integer powers other than 8 one more estimator call gives it).
+template <int M>
+__global__ void __launch_bounds__(128) k_de_spatial_grad(ShapeDev s, const float* __restrict__ pts,
+                                                         uint64_t n, float* __restrict__ out) {
+    __shared__ __align__(16) float stage[4][96];
+    const WarpWalk w = warp_walk();
+    const bool vec = (((uintptr_t)out) & 15u) == 0;
+    for (uint64_t base = w.first; base < n; base += w.stride) {
+        float x = 0.0f, y = 0.0f, z = 0.0f;
+        if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
+        float g[4];
+        shape_gradient<M>(s, x, y, z, g);
+        if constexpr (M == MODE_INT) g[0] = eval<M>(s, x, y, z);  // the estimator's bits
+        float* dst = out + 4 * (base + (threadIdx.x & 31));
+        if (vec) {
+            *reinterpret_cast<float4*>(dst) = make_float4(g[0], g[1], g[2], g[3]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) dst[k] = g[k];
+        }
     }
 }
 
@@ -190,6 +216,27 @@ cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_
     default: k_de_grad_tangent<4, true><<<G, 128, 0, st>>>(sd, dm, points, n, out); break;
     }
     CG_CHECK_LAUNCH("k_de_grad_tangent");
+    return CG_OK;
+}
+
+cg_status cg_de_spatial_grad(const cg_shape* shape, const float* points, uint64_t n, float* out,
+                             void* stream) {
+    CG_TRY(check_shape(shape));
+    if (n && (!points || !out)) {
+        set_error("NULL buffer");
+        return CG_EINVAL;
+    }
+    if (!n) return CG_OK;
+    const ShapeDev sd = make_shape_dev(*shape);
+    const unsigned G = grid_for(n, 128, 16);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (mode_of(sd, CG_NUMERICS_EXACT)) {
+    case MODE_P8: k_de_spatial_grad<MODE_P8><<<G, 128, 0, st>>>(sd, points, n, out); break;
+    case MODE_INT: k_de_spatial_grad<MODE_INT><<<G, 128, 0, st>>>(sd, points, n, out); break;
+    case MODE_POLAR: k_de_spatial_grad<MODE_POLAR><<<G, 128, 0, st>>>(sd, points, n, out); break;
+    default: k_de_spatial_grad<MODE_SPHERE><<<G, 128, 0, st>>>(sd, points, n, out); break;
+    }
+    CG_CHECK_LAUNCH("k_de_spatial_grad");
     return CG_OK;
 }
 

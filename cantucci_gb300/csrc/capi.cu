@@ -155,12 +155,21 @@ struct cg_mesher {
     MeshCounters* hcnt = nullptr;  // pinned
     uint32_t normals = CG_NORMALS_FD;
     uint32_t root_iters = 0;  // CG_CROSSINGS_LERP
+    uint32_t placement = CG_PLACEMENT_CENTROID;
     uint32_t last_res = 0;
     MeshWork last_w{};
     std::mutex mu;
 };
 
 namespace {
+
+PlaceOptions place_options(const cg_mesher* m) {
+    PlaceOptions o;
+    o.analytic_normals = m->normals == CG_NORMALS_ADJOINT;
+    o.root_iters = m->root_iters;
+    o.qef = m->placement == CG_PLACEMENT_QEF;
+    return o;
+}
 
 cg_status ensure(void** p, size_t* cap, size_t bytes) {
     if (*cap >= bytes && *p) return CG_OK;
@@ -208,9 +217,7 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     const SideStream side = {m->copy_stream, m->fork, m->join};
     CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
-                                  /*signs_ready=*/true,
-                                  /*analytic_normals=*/m->normals == CG_NORMALS_ADJOINT,
-                                  m->root_iters, &side));
+                                  /*signs_ready=*/true, place_options(m), &side));
     CG_CUDA(cudaEventRecord(m->ev[3], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -269,8 +276,7 @@ cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* sh
     CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     CG_TRY(launch_mesh_to_host(s, su, d, w, hverts_dev, vcap, m->didx, hidx, idev, st,
-                               m->copy_stream, m->ev[2], m->ev[3], m->hcnt,
-                               m->normals == CG_NORMALS_ADJOINT, m->root_iters));
+                               m->copy_stream, m->ev[2], m->ev[3], m->hcnt, place_options(m)));
     CG_CUDA(cudaEventRecord(m->ev[4], st));
     CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaStreamSynchronize(st));
@@ -435,6 +441,16 @@ cg_status cg_mesher_set_crossings(cg_mesher* m, uint32_t crossings, uint32_t ite
     }
     std::lock_guard<std::mutex> lk(m->mu);
     m->root_iters = crossings == CG_CROSSINGS_ROOT ? iters : 0;
+    return CG_OK;
+}
+
+cg_status cg_mesher_set_placement(cg_mesher* m, uint32_t placement) {
+    if (!m || placement > CG_PLACEMENT_QEF) {
+        set_error("placement: CG_PLACEMENT_CENTROID or CG_PLACEMENT_QEF");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(m->mu);
+    m->placement = placement;
     return CG_OK;
 }
 

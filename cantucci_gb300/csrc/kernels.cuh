@@ -85,11 +85,20 @@ MeshDims mesh_dims(uint32_t res);
 // Byte size of a workspace for `res`; fills `w` with offsets from `base`.
 size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 
+// Vertex placement options of the span mesher; the defaults are the
+// reference's placement.  analytic_normals (polar form only) replaces the
+// six-sample normal by the forward-mode gradient; root_iters > 0 places edge
+// crossings at the DE's root along each edge; qef places the vertex at the
+// dual-contouring minimiser of the crossings' tangent planes.
+struct PlaceOptions {
+    bool analytic_normals = false;
+    uint32_t root_iters = 0;
+    bool qef = false;
+};
+
 // Steps 2 and 3 of naive_surface_nets on a filled `dists` grid (and, with
 // signs_ready, filled sign words).  Output arrays are written only up to
-// their capacity; counts land in w.counters.  analytic_normals (polar form
-// only) replaces the six-sample normal by the forward-mode gradient;
-// root_iters > 0 places edge crossings at the DE's root along each edge.
+// their capacity; counts land in w.counters.
 // A second stream and a fork / join event pair: with it the quad indices
 // are built concurrently with the vertex placement.
 struct SideStream {
@@ -100,7 +109,7 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals = false, uint32_t root_iters = 0,
+                                 const PlaceOptions& opt = PlaceOptions(),
                                  const SideStream* side = nullptr);
 
 // The same steps for a mesh whose outputs go to host memory, reordered so
@@ -113,8 +122,8 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
                               const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
                               uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,
                               cudaStream_t st, cudaStream_t copy_st, cudaEvent_t ev_counts,
-                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals,
-                              uint32_t root_iters);
+                              cudaEvent_t ev_quads, MeshCounters* hcnt,
+                              const PlaceOptions& opt);
 
 // Cell -> vertex id table of the last mesh (0xFFFFFFFF off the surface).
 cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* points,

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
 // vertices and stores them through shared memory as 16-byte chunks (32
 // vertices = 896 bytes = 56 float4), so the stores are coalesced whether
 // `verts` is device memory or pinned host memory written over the C2C link.
-template <int M, bool AN, bool ROOT>
+template <int M, bool AN, bool ROOT, bool QEF>
 __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshDims d,
                                                const float* __restrict__ dists,
                                                const uint32_t* __restrict__ cellidx,
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
          base += gridDim.x * blockDim.x) {
         const uint32_t v = base + lane;
         float o[7] = {0, 0, 0, 0, 0, 0, 0};
-        if (v < V) bad |= !place_vertex<M, AN, ROOT>(s, pp, d, dists, cellidx[v], o, root_iters);
+        if (v < V) bad |= !place_vertex<M, AN, ROOT, QEF>(s, pp, d, dists, cellidx[v], o, root_iters);
 #pragma unroll
         for (int k = 0; k < 7; ++k) st[lane * 7 + k] = o[k];
         __syncwarp();
@@ -184,39 +184,49 @@ PlaceParams place_params(const SpanSetup& su) {
     return pp;
 }
 
-template <int M, bool AN>
-static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
-                              const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                              cudaStream_t st, uint32_t root_iters) {
+template <int M, bool AN, bool QEF>
+static void launch_place_qef(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
+                             const MeshWork& w, cg_vertex* verts, uint64_t vcap, cudaStream_t st,
+                             uint32_t root_iters) {
     const unsigned B = 128;
     const unsigned G = (unsigned)sm_count() * 16;
     if (root_iters)
-        k_place<M, AN, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                              vcap, root_iters);
+        k_place<M, AN, true, QEF><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                   verts, vcap, root_iters);
     else
-        k_place<M, AN, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters, verts,
-                                               vcap, 0);
+        k_place<M, AN, false, QEF><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                    verts, vcap, 0);
+}
+
+template <int M, bool AN>
+static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
+                              const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                              cudaStream_t st, const PlaceOptions& opt) {
+    if (opt.qef)
+        launch_place_qef<M, AN, true>(s, pp, d, w, verts, vcap, st, opt.root_iters);
+    else
+        launch_place_qef<M, AN, false>(s, pp, d, w, verts, vcap, st, opt.root_iters);
 }
 
 static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                              cudaStream_t st, bool analytic_normals, uint32_t root_iters) {
+                              cudaStream_t st, const PlaceOptions& opt) {
     const PlaceParams pp = place_params(su);
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
     case MODE_P8:
-        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, root_iters);
+        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, opt);
         break;
     case MODE_INT:
-        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, root_iters);
+        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, opt);
         break;
     case MODE_POLAR:
-        if (analytic_normals)
-            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, root_iters);
+        if (opt.analytic_normals)
+            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, opt);
         else
-            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, root_iters);
+            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, opt);
         break;
     default:
-        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, root_iters);
+        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, opt);
         break;
     }
     CG_CHECK_LAUNCH("k_place");
@@ -271,8 +281,7 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                  uint32_t* idx, uint64_t icap, cudaStream_t st,
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
-                                 bool analytic_normals, uint32_t root_iters,
-                                 const SideStream* side) {
+                                 const PlaceOptions& opt, const SideStream* side) {
     CG_TRY(launch_cells(d, w, st, signs_ready));
     if (side) {
         // The quads need only the cell table and the signs: they run on the
@@ -282,12 +291,12 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
         CG_TRY(launch_quad_count(d, w, side->stream));
         CG_TRY(launch_quad_emit(d, w, idx, icap, side->stream));
         CG_CUDA(cudaEventRecord(side->join, side->stream));
-        CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals, root_iters));
+        CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt));
         if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
         CG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
         return CG_OK;
     }
-    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, analytic_normals, root_iters));
+    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt));
     if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
     CG_TRY(launch_quad_count(d, w, st));
     CG_TRY(launch_quad_emit(d, w, idx, icap, st));
@@ -298,8 +307,8 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
                               const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
                               uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,
                               cudaStream_t st, cudaStream_t copy_st, cudaEvent_t ev_counts,
-                              cudaEvent_t ev_quads, MeshCounters* hcnt, bool analytic_normals,
-                              uint32_t root_iters) {
+                              cudaEvent_t ev_quads, MeshCounters* hcnt,
+                              const PlaceOptions& opt) {
     CG_TRY(launch_cells(d, w, st, /*signs_ready=*/true));
     CG_TRY(launch_quad_count(d, w, st));
     CG_CUDA(cudaMemcpyAsync(hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
@@ -314,7 +323,7 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     if (ci)
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 copy_st));
-    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, analytic_normals, root_iters));
+    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, opt));
     return CG_OK;
 }
 

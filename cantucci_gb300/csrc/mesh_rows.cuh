@@ -19,6 +19,7 @@
 #include "adjoint.cuh"
 #include "de.cuh"
 #include "kernels.cuh"
+#include "qef.cuh"
 
 namespace cg {
 
@@ -99,6 +100,46 @@ __device__ __forceinline__ float pick8(const float (&dd)[8], uint32_t k) {
 constexpr uint64_t kEdgeFrom = 0x642054103210ull;  // 0,1,2,3, 0,1,4,5, 0,2,4,6
 constexpr uint64_t kEdgeTo = 0x753176327654ull;    // 4,5,6,7, 2,3,6,7, 1,3,5,7
 
+// The reference's crossing on edge (from, to) of a cell with first corner
+// p0 (buffer.rs:187-250): the factor w = (d_from + delta) / delta, delta =
+// d_to - d_from, after the distances are oriented so that d_from < 0 (0.5
+// for equal distances), then Point3::lerp a (1 - w) + b w (src/math.rs:
+// 45-49).  A factor outside [0, 1] (math.rs:19 panics there) sets `bad`
+// and uses 0.
+__device__ __forceinline__ void lerp_crossing(const PlaceParams& pp, float p0x, float p0y,
+                                              float p0z, int from, int to, float df0, float dt0,
+                                              bool& bad, float& cx, float& cy, float& cz) {
+    float df, dt;
+    if (df0 < 0.0f) {
+        df = df0;
+        dt = dt0;
+    } else {
+        df = -df0;
+        dt = -dt0;
+    }
+    float wgt;
+    if (dt == df) {
+        wgt = 0.5f;
+    } else {
+        const float delta = __fsub_rn(dt, df);
+        wgt = __fdiv_rn(__fadd_rn(df, delta), delta);
+    }
+    if (!(wgt >= 0.0f && wgt <= 1.0f)) {
+        bad = true;
+        wgt = 0.0f;
+    }
+    const float ax = __fadd_rn(p0x, ((from >> 2) & 1) ? pp.step[0] : 0.0f);
+    const float ay = __fadd_rn(p0y, ((from >> 1) & 1) ? pp.step[1] : 0.0f);
+    const float az = __fadd_rn(p0z, (from & 1) ? pp.step[2] : 0.0f);
+    const float bx = __fadd_rn(p0x, ((to >> 2) & 1) ? pp.step[0] : 0.0f);
+    const float by = __fadd_rn(p0y, ((to >> 1) & 1) ? pp.step[1] : 0.0f);
+    const float bz = __fadd_rn(p0z, (to & 1) ? pp.step[2] : 0.0f);
+    const float omt = __fsub_rn(1.0f, wgt);
+    cx = __fadd_rn(__fmul_rn(ax, omt), __fmul_rn(bx, wgt));
+    cy = __fadd_rn(__fmul_rn(ay, omt), __fmul_rn(by, wgt));
+    cz = __fadd_rn(__fmul_rn(az, omt), __fmul_rn(bz, wgt));
+}
+
 // Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
 // crossings, DE at the vertex and the six-sample central-difference normal.
 // With AN (polar form only) the normal is instead the normalised analytic
@@ -107,9 +148,15 @@ constexpr uint64_t kEdgeTo = 0x753176327654ull;    // 4,5,6,7, 2,3,6,7, 1,3,5,7
 // reference's distance-weighted lerp but the root of the DE along the edge,
 // found by root_iters Illinois (regula falsi) steps from the edge's corner
 // distances -- the refinement buffer.rs:178-186 leaves for
-// later (issue #1); the cell table and the index list do not change.
+// later (issue #1).  With QEF the vertex is not the crossings' centroid but
+// the dual-contouring minimiser of their tangent planes (qef.cuh; issue #2),
+// with each plane's normal from one forward-mode gradient at its crossing;
+// its crossings are the roots (ROOT) or the zeros of the linear interpolant
+// of the corner distances, not the reference's lerp points, which sit
+// mirrored about the edge midpoint.
+// Neither changes the cell table or the index list.
 // Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
-template <int M, bool AN = false, bool ROOT = false>
+template <int M, bool AN = false, bool ROOT = false, bool QEF = false>
 __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
                                              const MeshDims& d, const float* __restrict__ dists,
                                              uint32_t c, float* __restrict__ o,
@@ -136,41 +183,16 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
         const float df0 = dd[from], dt0 = dd[to];
         if ((__float_as_uint(df0) >> 31) == (__float_as_uint(dt0) >> 31)) continue;
         xmask |= 1u << k;
-        float df, dt;
-        if (df0 < 0.0f) {
-            df = df0;
-            dt = dt0;
-        } else {
-            df = -df0;
-            dt = -dt0;
-        }
-        float wgt;
-        if (dt == df) {
-            wgt = 0.5f;
-        } else {
-            const float delta = __fsub_rn(dt, df);
-            wgt = __fdiv_rn(__fadd_rn(df, delta), delta);
-        }
-        // math::lerp asserts 0 <= t <= 1 (src/math.rs:19).
-        if (!(wgt >= 0.0f && wgt <= 1.0f)) {
-            bad = true;
-            wgt = 0.0f;
-        }
-        const float ax = __fadd_rn(p0x, ((from >> 2) & 1) ? pp.step[0] : 0.0f);
-        const float ay = __fadd_rn(p0y, ((from >> 1) & 1) ? pp.step[1] : 0.0f);
-        const float az = __fadd_rn(p0z, (from & 1) ? pp.step[2] : 0.0f);
-        const float bx = __fadd_rn(p0x, ((to >> 2) & 1) ? pp.step[0] : 0.0f);
-        const float by = __fadd_rn(p0y, ((to >> 1) & 1) ? pp.step[1] : 0.0f);
-        const float bz = __fadd_rn(p0z, (to & 1) ? pp.step[2] : 0.0f);
-        // Point3::lerp: self * (1 - t) + other * t (src/math.rs:45-49).
-        const float omt = __fsub_rn(1.0f, wgt);
-        sx = __fadd_rn(sx, __fadd_rn(__fmul_rn(ax, omt), __fmul_rn(bx, wgt)));
-        sy = __fadd_rn(sy, __fadd_rn(__fmul_rn(ay, omt), __fmul_rn(by, wgt)));
-        sz = __fadd_rn(sz, __fadd_rn(__fmul_rn(az, omt), __fmul_rn(bz, wgt)));
+        float cx, cy, cz;
+        lerp_crossing(pp, p0x, p0y, p0z, from, to, df0, dt0, bad, cx, cy, cz);
+        sx = __fadd_rn(sx, cx);
+        sy = __fadd_rn(sy, cy);
+        sz = __fadd_rn(sz, cz);
         ++count;
     }
-    if constexpr (ROOT) {
-        sx = sy = sz = 0.0f;
+    Qef q = {};
+    if constexpr (ROOT || QEF) {
+        if constexpr (ROOT) sx = sy = sz = 0.0f;
 #pragma unroll 1
         for (uint32_t m = xmask; m; m &= m - 1) {
             const uint32_t k = __ffs(m) - 1;
@@ -183,35 +205,60 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
             const float ey = (((to >> 1) & 1) ? pp.step[1] : 0.0f) - (((from >> 1) & 1) ? pp.step[1] : 0.0f);
             const float ez = ((to & 1) ? pp.step[2] : 0.0f) - ((from & 1) ? pp.step[2] : 0.0f);
             float f0 = pick8(dd, from), f1 = pick8(dd, to);
-            const uint32_t in0 = __float_as_uint(f0) >> 31;  // the sign bit: NaN counts as inside
-            float t0 = 0.0f, t1 = 1.0f, t = 0.5f;
-            int side = 0;
-            for (uint32_t it = 0; it < root_iters; ++it) {
-                float tc = (t0 * f1 - t1 * f0) / (f1 - f0);
-                if (!(tc > t0 && tc < t1)) tc = 0.5f * (t0 + t1);  // NaN or degenerate: bisect
-                const float fc = eval<M>(s, ax + tc * ex, ay + tc * ey, az + tc * ez);
-                if ((__float_as_uint(fc) >> 31) == in0) {
-                    t0 = tc;
-                    f0 = fc;
-                    if (side == -1) f1 *= 0.5f;
-                    side = -1;
-                } else {
-                    t1 = tc;
-                    f1 = fc;
-                    if (side == 1) f0 *= 0.5f;
-                    side = 1;
+            float t;
+            if constexpr (ROOT) {
+                const uint32_t in0 = __float_as_uint(f0) >> 31;  // the sign bit: NaN counts as inside
+                float t0 = 0.0f, t1 = 1.0f;
+                int side = 0;
+                t = 0.5f;
+                for (uint32_t it = 0; it < root_iters; ++it) {
+                    float tc = (t0 * f1 - t1 * f0) / (f1 - f0);
+                    if (!(tc > t0 && tc < t1)) tc = 0.5f * (t0 + t1);  // NaN or degenerate: bisect
+                    const float fc = eval<M>(s, ax + tc * ex, ay + tc * ey, az + tc * ez);
+                    if ((__float_as_uint(fc) >> 31) == in0) {
+                        t0 = tc;
+                        f0 = fc;
+                        if (side == -1) f1 *= 0.5f;
+                        side = -1;
+                    } else {
+                        t1 = tc;
+                        f1 = fc;
+                        if (side == 1) f0 *= 0.5f;
+                        side = 1;
+                    }
+                    t = tc;
                 }
-                t = tc;
+            } else {
+                // The zero of the linear interpolant of the corner distances.
+                // (The reference's lerp above sits at 1 - t: its weight
+                // d_to / (d_to - d_from) multiplies the `to` corner.)
+                t = f0 / (f0 - f1);
+                if (!(t >= 0.0f && t <= 1.0f)) t = 0.5f;
             }
-            sx += ax + t * ex;
-            sy += ay + t * ey;
-            sz += az + t * ez;
+            const float cx = ax + t * ex, cy = ay + t * ey, cz = az + t * ez;
+            if constexpr (ROOT) {
+                sx += cx;
+                sy += cy;
+                sz += cz;
+            }
+            if constexpr (QEF) {
+                float g[4];
+                shape_gradient<M>(s, cx, cy, cz, g);
+                qef_add(q, cx - p0x, cy - p0y, cz - p0z, g[1], g[2], g[3]);
+            }
         }
     }
     const float cf = (float)count;
-    const float vx = __fadd_rn(0.0f, __fdiv_rn(sx, cf));
-    const float vy = __fadd_rn(0.0f, __fdiv_rn(sy, cf));
-    const float vz = __fadd_rn(0.0f, __fdiv_rn(sz, cf));
+    float vx = __fadd_rn(0.0f, __fdiv_rn(sx, cf));
+    float vy = __fadd_rn(0.0f, __fdiv_rn(sy, cf));
+    float vz = __fadd_rn(0.0f, __fdiv_rn(sz, cf));
+    if constexpr (QEF) {
+        float rx, ry, rz;
+        qef_solve(q, pp.step[0], pp.step[1], pp.step[2], rx, ry, rz);
+        vx = p0x + rx;
+        vy = p0y + ry;
+        vz = p0z + rz;
+    }
     // Sample 0 is the vertex; samples 1..6 are p + unit * (+-delta) along
     // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
     // loop is kept rolled so that one copy of the estimator is in the code.

@@ -1,0 +1,267 @@
+// qef.cuh -- the spatial gradient of every shape's estimator in forward
+// mode, and the quadratic-error vertex of dual contouring built on it.
+//
+// Dual contouring (Ju, Losasso, Schaefer and Warren, "Dual Contouring of
+// Hermite Data", SIGGRAPH 2002) is the placement src/mesh/buffer.rs:53-54
+// names as the successor of naive surface nets (reference issue #2): a
+// cell's vertex minimises the summed squared distance to the tangent planes
+// at its edge crossings,
+//     E(x) = sum_i (n_i . (x - p_i))^2,
+// instead of sitting at the crossings' centroid, so creases and thin parts
+// of the surface are not rounded off.  The cell table and the quads do not
+// change: only the vertex inside each surface cell moves.
+#pragma once
+
+#include <cstdint>
+
+#include "adjoint.cuh"
+#include "de.cuh"
+
+namespace cg {
+
+// A value and its derivatives along x, y, z of the evaluated point.  The
+// value channel uses the estimator's exact operations (IEEE, uncontracted),
+// so the escape test and the z-axis test branch exactly as the estimator
+// does; the derivative channels use contracted arithmetic.
+struct D3 {
+    float v, d0, d1, d2;
+};
+
+__device__ __forceinline__ D3 d3c(float v) { return {v, 0.0f, 0.0f, 0.0f}; }
+__device__ __forceinline__ D3 d3add(const D3& a, const D3& b) {
+    return {__fadd_rn(a.v, b.v), a.d0 + b.d0, a.d1 + b.d1, a.d2 + b.d2};
+}
+__device__ __forceinline__ D3 d3sub(const D3& a, const D3& b) {
+    return {__fsub_rn(a.v, b.v), a.d0 - b.d0, a.d1 - b.d1, a.d2 - b.d2};
+}
+__device__ __forceinline__ D3 d3mul(const D3& a, const D3& b) {
+    return {__fmul_rn(a.v, b.v), fmaf(a.d0, b.v, a.v * b.d0), fmaf(a.d1, b.v, a.v * b.d1),
+            fmaf(a.d2, b.v, a.v * b.d2)};
+}
+__device__ __forceinline__ D3 d3scale(float c, const D3& a) {
+    return {__fmul_rn(c, a.v), c * a.d0, c * a.d1, c * a.d2};
+}
+__device__ __forceinline__ D3 d3div(const D3& a, const D3& b) {
+    const float q = __fdiv_rn(a.v, b.v), inv = 1.0f / b.v;
+    return {q, (a.d0 - q * b.d0) * inv, (a.d1 - q * b.d1) * inv, (a.d2 - q * b.d2) * inv};
+}
+__device__ __forceinline__ D3 d3sqrt(const D3& a) {
+    const float s = __fsqrt_rn(a.v), h = 0.5f / s;
+    return {s, a.d0 * h, a.d1 * h, a.d2 * h};
+}
+
+// Forward-mode tangent of Mandelbulb::min_distance_from for P = 8
+// (src/shape/mandelbulb.rs:59-79) through rotate_inner_p8_scalar
+// (mandelbulb.rs:148-200) exactly as written.  That polynomial is not the
+// polar map (its x' subtracts y^8 where Re((x + iy)^8) adds it), so the
+// polar tangent would differentiate another function.  On the z axis
+// (rotate_on_z_axis, mandelbulb.rs:114-126) z' = r^8 cos(8 acos(+-1)) = r^8,
+// whose derivative is 8 r^7 r'.  g[0] = DE (the estimator's bits), g[1..3] =
+// dDE/dp; DE' = 0.5 (ln r + 1) r' / dr - DE dr' / dr at the returned (stale
+// or escaping) r.
+static __device__ __noinline__ void p8_de_gradient(uint32_t max_iters, float bailout, float px,
+                                                   float py, float pz, float* g) {
+    const D3 qx = {px, 1.0f, 0.0f, 0.0f}, qy = {py, 0.0f, 1.0f, 0.0f}, qz = {pz, 0.0f, 0.0f, 1.0f};
+    D3 x = qx, y = qy, z = qz, dr = d3c(1.0f), r = d3c(0.0f);
+    for (uint32_t i = 0; i < max_iters; ++i) {
+        r = d3sqrt(d3add(d3add(d3mul(x, x), d3mul(y, y)), d3mul(z, z)));
+        if (r.v > bailout) break;
+        // f32::powi(r, 7) = (r * r^2) * r^4, times P, times dr, plus 1
+        const D3 r2 = d3mul(r, r), r4 = d3mul(r2, r2), r7 = d3mul(d3mul(r, r2), r4);
+        dr = d3add(d3mul(d3scale(8.0f, r7), dr), d3c(1.0f));
+        D3 nx, ny, nz;
+        if (on_z_axis(x.v, y.v)) {
+            nx = d3c(0.0f);
+            ny = d3c(0.0f);
+            const float k = 8.0f * r7.v;
+            nz = {rotate_axis_z<Exact>(8, x.v, y.v, z.v), k * r.d0, k * r.d1, k * r.d2};
+        } else {
+            const D3 x2 = d3mul(x, x), x4 = d3mul(x2, x2), x6 = d3mul(x4, x2), x8 = d3mul(x4, x4);
+            const D3 y2 = d3mul(y, y), y4 = d3mul(y2, y2), y6 = d3mul(y4, y2), y8 = d3mul(y4, y4);
+            const D3 z2 = d3mul(z, z), z4 = d3mul(z2, z2), z6 = d3mul(z4, z2), z8 = d3mul(z4, z4);
+            const D3 rxy2 = d3add(x2, y2);
+            const D3 rxy4 = d3mul(rxy2, rxy2);
+            const D3 rxy6 = d3mul(rxy2, rxy4);
+            const D3 rxy8 = d3mul(rxy4, rxy4);
+            const D3 num = d3sub(d3add(d3sub(z8, d3mul(d3scale(28.0f, z6), rxy2)),
+                                       d3mul(d3scale(70.0f, z4), rxy4)),
+                                 d3mul(d3scale(28.0f, z2), rxy6));
+            const D3 a = d3add(d3c(1.0f), d3div(num, rxy8));
+            const D3 X = d3sub(d3sub(d3add(d3sub(x8, d3mul(d3scale(28.0f, x6), y2)),
+                                           d3mul(d3scale(70.0f, x4), y4)),
+                                     d3mul(d3scale(28.0f, x2), y6)),
+                               y8);
+            nx = d3mul(a, X);
+            const D3 Y = d3sub(d3add(d3sub(x6, d3mul(d3scale(7.0f, x4), y2)),
+                                     d3mul(d3scale(7.0f, x2), y4)),
+                               y6);
+            ny = d3mul(d3mul(d3mul(d3scale(8.0f, a), x), y), Y);
+            const D3 Z = d3add(d3sub(z4, d3mul(d3scale(6.0f, z2), rxy2)), rxy4);
+            nz = d3mul(d3mul(d3mul(d3scale(8.0f, z), d3sqrt(rxy2)), d3sub(z2, rxy2)), Z);
+        }
+        x = d3add(nx, qx);
+        y = d3add(ny, qy);
+        z = d3add(nz, qz);
+    }
+    const float ln_r = logf(r.v);
+    const float de = __fdiv_rn(__fmul_rn(0.5f, __fmul_rn(ln_r, r.v)), dr.v);
+    const float c_r = 0.5f * (ln_r + 1.0f) / dr.v, c_dr = -de / dr.v;
+    g[0] = x86_nan(de);
+    g[1] = c_r * r.d0 + c_dr * dr.d0;
+    g[2] = c_r * r.d1 + c_dr * dr.d1;
+    g[3] = c_r * r.d2 + c_dr * dr.d2;
+}
+
+// DE and dDE/dp of the shape in g[0..3], one forward-mode pass:
+//   Sphere (src/shape/sphere.rs:33-35): (p - c) / |p - c|;
+//   Mandelbulb, P = 8: p8_de_gradient;
+//   Mandelbulb, other integer P (rotate_inner_px_generic, mandelbulb.rs:
+//     128-146): the polar map with power P and no rotation -- the same
+//     function -- so polar_de_tangent, whose g[0] is then the polar form's
+//     f32 value (libm rounding apart, the estimator's);
+//   polar Mandelbulb: polar_de_tangent.
+template <int M>
+__device__ __forceinline__ void shape_gradient(const ShapeDev& s, float x, float y, float z,
+                                               float* g) {
+    if constexpr (M == MODE_SPHERE) {
+        const float dx = x - s.center[0], dy = y - s.center[1], dz = z - s.center[2];
+        const float l = sqrtf(dx * dx + dy * dy + dz * dz);
+        const float inv = 1.0f / l;
+        g[0] = sphere_de(s, x, y, z);
+        g[1] = dx * inv;
+        g[2] = dy * inv;
+        g[3] = dz * inv;
+    } else if constexpr (M == MODE_P8 || M == MODE_P8_FAST) {
+        p8_de_gradient(s.max_iters, s.bailout, x, y, z, g);
+    } else {
+        float o[5];
+        if constexpr (M == MODE_INT || M == MODE_INT_POLY) {
+            ShapeDev t = s;
+            t.power_f = (float)s.power;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) t.m[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+            polar_de_tangent<3, false>(t, nullptr, x, y, z, o);
+        } else {
+            polar_de_tangent<3, false>(s, nullptr, x, y, z, o);
+        }
+        g[0] = o[0];
+        g[1] = o[1];
+        g[2] = o[2];
+        g[3] = o[3];
+    }
+}
+
+// Eigenvalues of A^T A below this fraction of the largest are dropped from
+// the pseudo-inverse (singular values of A below 10% of the largest, the
+// truncation Ju et al. use): along a direction the planes barely constrain,
+// the vertex stays at the mass point.
+constexpr float kQefTruncate = 0.01f;
+
+// The quadratic error of one cell, accumulated crossing by crossing in
+// coordinates relative to the cell's first corner: A^T A (6 entries of the
+// symmetric 3x3), A^T b with b_i = n_i . p_i, and the crossing sum for the
+// mass point.  A crossing whose gradient is zero or not finite adds its
+// point to the mass point but no plane.
+struct Qef {
+    float a00, a01, a02, a11, a12, a22;
+    float b0, b1, b2;
+    float mx, my, mz;
+    uint32_t points, planes;
+};
+
+__device__ __forceinline__ void qef_add(Qef& q, float rx, float ry, float rz, float gx, float gy,
+                                        float gz) {
+    q.mx += rx;
+    q.my += ry;
+    q.mz += rz;
+    ++q.points;
+    const float l2 = gx * gx + gy * gy + gz * gz;
+    if (!(l2 > 0.0f) || !(l2 < 3.0e38f)) return;
+    const float inv = rsqrtf(l2);
+    const float nx = gx * inv, ny = gy * inv, nz = gz * inv;
+    const float b = nx * rx + ny * ry + nz * rz;
+    q.a00 += nx * nx;
+    q.a01 += nx * ny;
+    q.a02 += nx * nz;
+    q.a11 += ny * ny;
+    q.a12 += ny * nz;
+    q.a22 += nz * nz;
+    q.b0 += nx * b;
+    q.b1 += ny * b;
+    q.b2 += nz * b;
+    ++q.planes;
+}
+
+// One Jacobi rotation of the cyclic Jacobi eigenvalue method (Golub and Van
+// Loan, Matrix Computations, section 8.5) on symmetric `a`, zeroing a[P][Q];
+// the rotation is accumulated into the eigenvector columns of `v`.
+template <int P, int Q>
+__device__ __forceinline__ void jacobi_rotate(float (&a)[3][3], float (&v)[3][3]) {
+    constexpr int R = 3 - P - Q;
+    const float apq = a[P][Q];
+    if (!(fabsf(apq) > 1e-30f)) return;
+    const float theta = 0.5f * (a[Q][Q] - a[P][P]) / apq;
+    float t = 1.0f / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.0f)));
+    if (theta < 0.0f) t = -t;
+    const float c = rsqrtf(fmaf(t, t, 1.0f)), sn = t * c;
+    a[P][P] -= t * apq;
+    a[Q][Q] += t * apq;
+    a[P][Q] = a[Q][P] = 0.0f;
+    const float arp = a[R][P], arq = a[R][Q];
+    a[R][P] = a[P][R] = c * arp - sn * arq;
+    a[R][Q] = a[Q][R] = sn * arp + c * arq;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float vp = v[k][P], vq = v[k][Q];
+        v[k][P] = c * vp - sn * vq;
+        v[k][Q] = sn * vp + c * vq;
+    }
+}
+
+// Minimiser of the cell's quadratic error, relative to its first corner:
+// x = c + pinv(A^T A) (A^T b - A^T A c) with c the mass point and the
+// truncated pseudo-inverse of kQefTruncate, then clamped to the cell
+// [0, h].  No planes, or a correction that is not finite: the mass point.
+__device__ __forceinline__ void qef_solve(const Qef& q, float hx, float hy, float hz, float& ox,
+                                          float& oy, float& oz) {
+    const float inv_n = 1.0f / (float)q.points;
+    const float cx = q.mx * inv_n, cy = q.my * inv_n, cz = q.mz * inv_n;
+    ox = cx;
+    oy = cy;
+    oz = cz;
+    if (q.planes) {
+        float a[3][3] = {{q.a00, q.a01, q.a02}, {q.a01, q.a11, q.a12}, {q.a02, q.a12, q.a22}};
+        const float r0 = q.b0 - (q.a00 * cx + q.a01 * cy + q.a02 * cz);
+        const float r1 = q.b1 - (q.a01 * cx + q.a11 * cy + q.a12 * cz);
+        const float r2 = q.b2 - (q.a02 * cx + q.a12 * cy + q.a22 * cz);
+        float v[3][3] = {{1.0f, 0.0f, 0.0f}, {0.0f, 1.0f, 0.0f}, {0.0f, 0.0f, 1.0f}};
+#pragma unroll
+        for (int sweep = 0; sweep < 5; ++sweep) {
+            jacobi_rotate<0, 1>(a, v);
+            jacobi_rotate<0, 2>(a, v);
+            jacobi_rotate<1, 2>(a, v);
+        }
+        const float lmax = fmaxf(a[0][0], fmaxf(a[1][1], a[2][2]));
+        float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float l = a[i][i];
+            if (l > kQefTruncate * lmax) {
+                const float c = (v[0][i] * r0 + v[1][i] * r1 + v[2][i] * r2) / l;
+                dx += c * v[0][i];
+                dy += c * v[1][i];
+                dz += c * v[2][i];
+            }
+        }
+        if (isfinite(dx) && isfinite(dy) && isfinite(dz)) {
+            ox += dx;
+            oy += dy;
+            oz += dz;
+        }
+    }
+    ox = fminf(fmaxf(ox, 0.0f), hx);
+    oy = fminf(fmaxf(oy, 0.0f), hy);
+    oz = fminf(fmaxf(oz, 0.0f), hz);
+}
+
+}  // namespace cg

@@ -68,6 +68,14 @@ enum {
     CG_CROSSINGS_ROOT = 1   /* the DE's root along the edge, regula falsi (new; issue #1) */
 };
 
+/* Where a surface cell's vertex goes (cg_mesher_set_placement). */
+enum {
+    CG_PLACEMENT_CENTROID = 0, /* centroid of the edge crossings: naive surface nets,
+                                  buffer.rs:149-252 */
+    CG_PLACEMENT_QEF = 1       /* dual contouring: minimiser of the squared distances to the
+                                  tangent planes at the crossings, buffer.rs:53-54 (new; issue #2) */
+};
+
 /* A shape; 48 bytes.  `power`/`max_iters`/`bailout` are Mandelbulb's fields
  * (src/shape/mandelbulb.rs:13-16; the reference's u64 max_iters fits u32 here). */
 typedef struct cg_shape {
@@ -158,6 +166,15 @@ cg_status cg_mesher_set_normals(cg_mesher* mesher, uint32_t normals);
  * buffer.rs:178-186 suggests; the cell table and index list are unchanged,
  * vertex positions (and so their DE and normals) move onto the surface. */
 cg_status cg_mesher_set_crossings(cg_mesher* mesher, uint32_t crossings, uint32_t iters);
+/* Select the vertex placement (CG_PLACEMENT_CENTROID default).  With
+ * CG_PLACEMENT_QEF each surface cell's vertex minimises sum_i (n_i . (x -
+ * p_i))^2 over the crossings p_i (lerped or root-found, as selected) and the
+ * unit gradients n_i of the DE there (one forward-mode pass per crossing),
+ * by a truncated pseudo-inverse (eigenvalues below 1% of the largest
+ * dropped) around the crossings' mass point, clamped to the cell.  The cell
+ * table and index list are unchanged; the DE and normal are evaluated at
+ * the new position.  Any shape. */
+cg_status cg_mesher_set_placement(cg_mesher* mesher, uint32_t placement);
 
 /* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.
  * Writes min(count, cap) items; if a count exceeds its capacity the call
@@ -432,6 +449,15 @@ cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, flo
 enum { CG_GRAD_POWER = 1, CG_GRAD_FAST = 2 };
 cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
                              uint32_t flags, float* out, void* stream);
+
+/* DE and its spatial gradient for any shape, one forward-mode pass per
+ * point (the gradient dual contouring uses).  out: device, n x 4 floats:
+ * DE (the estimator's, bit for bit), dDE/dx, dDE/dy, dDE/dz.  Mandelbulb
+ * P = 8 differentiates rotate_inner_p8_scalar (mandelbulb.rs:148-200) as
+ * written; other integer powers the equal polar map; Sphere (p - c) /
+ * |p - c|.  No reference counterpart. */
+cg_status cg_de_spatial_grad(const cg_shape* shape, const float* points, uint64_t n, float* out,
+                             void* stream);
 
 /* Backward of DE over a batch (the autograd.Function backward): given the
  * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to

@@ -182,6 +182,8 @@ public:
     void set_crossings(uint32_t crossings, uint32_t iters = 4) {
         check(cg_mesher_set_crossings(m_, crossings, iters));
     }
+    // CG_PLACEMENT_CENTROID (the reference's) or CG_PLACEMENT_QEF (dual contouring).
+    void set_placement(uint32_t placement) { check(cg_mesher_set_placement(m_, placement)); }
 
     static Mesher& for_this_thread() {
         thread_local Mesher m(0);
