@@ -156,6 +156,7 @@ struct cg_mesher {
     uint32_t normals = CG_NORMALS_FD;
     uint32_t root_iters = 0;  // CG_CROSSINGS_LERP
     uint32_t placement = CG_PLACEMENT_CENTROID;
+    DeviceScratch edge_rows, edge_data;  // dual contouring's edge table
     uint32_t last_res = 0;
     MeshWork last_w{};
     std::mutex mu;
@@ -163,11 +164,13 @@ struct cg_mesher {
 
 namespace {
 
-PlaceOptions place_options(const cg_mesher* m) {
+PlaceOptions place_options(cg_mesher* m) {
     PlaceOptions o;
     o.analytic_normals = m->normals == CG_NORMALS_ADJOINT;
     o.root_iters = m->root_iters;
     o.qef = m->placement == CG_PLACEMENT_QEF;
+    o.edge_rows = &m->edge_rows;
+    o.edge_data = &m->edge_data;
     return o;
 }
 
@@ -414,6 +417,8 @@ void cg_mesher_destroy(cg_mesher* m) {
     if (m->dverts) cudaFree(m->dverts);
     if (m->didx) cudaFree(m->didx);
     if (m->hcnt) cudaFreeHost(m->hcnt);
+    if (m->edge_rows.ptr) cudaFree(m->edge_rows.ptr);
+    if (m->edge_data.ptr) cudaFree(m->edge_data.ptr);
     for (auto& e : m->ev)
         if (e) cudaEventDestroy(e);
     if (m->fork) cudaEventDestroy(m->fork);

@@ -59,7 +59,7 @@ struct MeshCounters {
     uint32_t vertices;  // surface cells
     uint32_t quads;     // faces
     uint32_t status;    // bit 0: a lerp factor left [0,1]
-    uint32_t pad;
+    uint32_t edges;     // sign-changing corner edges (dual contouring's edge table)
 };
 enum : uint32_t { MESH_LERP_FAIL = 1u };
 
@@ -90,10 +90,23 @@ size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 // six-sample normal by the forward-mode gradient; root_iters > 0 places edge
 // crossings at the DE's root along each edge; qef places the vertex at the
 // dual-contouring minimiser of the crossings' tangent planes.
+// A grow-only device buffer owned by the caller.
+struct DeviceScratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+cg_status grow_scratch(DeviceScratch* b, size_t bytes);
+
+// With qef the crossings go into an edge table first (one crossing and
+// gradient per sign-changing edge, shared by the edge's cells): its per-row
+// part lives in edge_rows, its per-edge part in edge_data; both are
+// required with qef.
 struct PlaceOptions {
     bool analytic_normals = false;
     uint32_t root_iters = 0;
     bool qef = false;
+    DeviceScratch* edge_rows = nullptr;
+    DeviceScratch* edge_data = nullptr;
 };
 
 // Steps 2 and 3 of naive_surface_nets on a filled `dists` grid (and, with

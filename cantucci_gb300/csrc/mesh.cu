@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
                                                const uint32_t* __restrict__ cellidx,
                                                MeshCounters* __restrict__ cnt,
                                                cg_vertex* __restrict__ verts, uint64_t vcap,
-                                               uint32_t root_iters) {
+                                               uint32_t root_iters, EdgeTable et) {
     __shared__ __align__(16) float stage[4][32 * 7];
     const uint32_t V = cnt->vertices;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
          base += gridDim.x * blockDim.x) {
         const uint32_t v = base + lane;
         float o[7] = {0, 0, 0, 0, 0, 0, 0};
-        if (v < V) bad |= !place_vertex<M, AN, ROOT, QEF>(s, pp, d, dists, cellidx[v], o, root_iters);
+        if (v < V) bad |= !place_vertex<M, AN, ROOT, QEF>(s, pp, d, dists, cellidx[v], o, root_iters, &et);
 #pragma unroll
         for (int k = 0; k < 7; ++k) st[lane * 7 + k] = o[k];
         __syncwarp();
@@ -126,6 +126,79 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
         __syncwarp();
     }
     if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
+}
+
+// Edge table, pass 1: per row r = a n^2 + x n + y (axis a, corner row
+// (x, y)), the sign-changing edges before each word and in the row.
+__global__ void __launch_bounds__(256) k_edge_rows(const uint32_t* __restrict__ sgn, MeshDims d,
+                                                   uint32_t* __restrict__ ewoff,
+                                                   uint32_t* __restrict__ ecount) {
+    const uint32_t n2 = d.n * d.n, rows = 3 * n2;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < d.W; ++w) {
+            ewoff[r * d.W + w] = run;
+            run += __popc(edge_bits(sgn, d, a, x, y, w));
+        }
+        ecount[r] = run;
+    }
+}
+
+// Pass 2: the edges in id order, each as the code r n + z.
+__global__ void __launch_bounds__(256) k_edge_list(const uint32_t* __restrict__ sgn, MeshDims d,
+                                                   const uint32_t* __restrict__ eoff,
+                                                   const uint32_t* __restrict__ ewoff,
+                                                   uint32_t* __restrict__ list) {
+    const uint32_t n2 = d.n * d.n, rows = 3 * n2;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x) {
+        const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
+        for (uint32_t w = 0; w < d.W; ++w) {
+            uint32_t bits = edge_bits(sgn, d, a, x, y, w);
+            uint32_t v = eoff[r] + ewoff[r * d.W + w];
+            while (bits) {
+                const uint32_t b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                list[v++] = r * d.n + w * 32 + b;
+            }
+        }
+    }
+}
+
+// Pass 3, one edge per thread: its crossing t (the root with ROOT, else the
+// zero of the linear interpolant of its corner distances) and the DE's
+// gradient there.
+template <int M, bool ROOT>
+__global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, MeshDims d,
+                                                   const float* __restrict__ dists,
+                                                   const uint32_t* __restrict__ list,
+                                                   const MeshCounters* __restrict__ cnt,
+                                                   float4* __restrict__ data, uint32_t root_iters) {
+    const uint32_t E = cnt->edges, n2 = d.n * d.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
+        const uint32_t code = list[i];
+        const uint32_t z = code % d.n, r = code / d.n;
+        const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
+        const uint32_t x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+        const float f0 = dists[((size_t)x * d.n + y) * d.n + z];
+        const float f1 = dists[((size_t)x1 * d.n + y1) * d.n + z1];
+        const float ax = __fadd_rn(pp.start[0], __fmul_rn((float)x, pp.step[0]));
+        const float ay = __fadd_rn(pp.start[1], __fmul_rn((float)y, pp.step[1]));
+        const float az = __fadd_rn(pp.start[2], __fmul_rn((float)z, pp.step[2]));
+        const float ex = a == 0 ? pp.step[0] : 0.0f;
+        const float ey = a == 1 ? pp.step[1] : 0.0f;
+        const float ez = a == 2 ? pp.step[2] : 0.0f;
+        float t;
+        if constexpr (ROOT)
+            t = root_on_edge<M>(s, ax, ay, az, ex, ey, ez, f0, f1, root_iters);
+        else
+            t = linear_root(f0, f1);
+        float g[4];
+        shape_gradient<M>(s, ax + t * ex, ay + t * ey, az + t * ez, g);
+        data[i] = make_float4(t, g[1], g[2], g[3]);
+    }
 }
 
 __global__ void __launch_bounds__(256) k_quad_count(const uint32_t* __restrict__ sgn, MeshDims d,
@@ -184,49 +257,132 @@ PlaceParams place_params(const SpanSetup& su) {
     return pp;
 }
 
-template <int M, bool AN, bool QEF>
-static void launch_place_qef(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
-                             const MeshWork& w, cg_vertex* verts, uint64_t vcap, cudaStream_t st,
-                             uint32_t root_iters) {
-    const unsigned B = 128;
-    const unsigned G = (unsigned)sm_count() * 16;
-    if (root_iters)
-        k_place<M, AN, true, QEF><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                   verts, vcap, root_iters);
-    else
-        k_place<M, AN, false, QEF><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                    verts, vcap, 0);
-}
-
 template <int M, bool AN>
 static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                              cudaStream_t st, const PlaceOptions& opt) {
+                              cudaStream_t st, const PlaceOptions& opt, const EdgeTable& et) {
+    const unsigned B = 128;
+    const unsigned G = (unsigned)sm_count() * 16;
     if (opt.qef)
-        launch_place_qef<M, AN, true>(s, pp, d, w, verts, vcap, st, opt.root_iters);
+        k_place<M, AN, false, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                     verts, vcap, 0, et);
+    else if (opt.root_iters)
+        k_place<M, AN, true, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                     verts, vcap, opt.root_iters, et);
     else
-        launch_place_qef<M, AN, false>(s, pp, d, w, verts, vcap, st, opt.root_iters);
+        k_place<M, AN, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                      verts, vcap, 0, et);
+}
+
+// The per-row part of the edge table for `res`: ecount, eoff (3 n^2 each),
+// ewoff (3 n^2 W) and the scan's block sums, in edge_rows.
+struct EdgeRows {
+    uint32_t *ecount, *eoff, *ewoff, *scratch;
+};
+
+static size_t edge_rows_layout(const MeshDims& d, char* base, EdgeRows* e) {
+    const size_t rows = 3ull * d.n * d.n;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += (bytes + 255) & ~(size_t)255;
+        return (uint32_t*)p;
+    };
+    EdgeRows t;
+    t.ecount = take(rows * 4);
+    t.eoff = take(rows * 4);
+    t.ewoff = take(rows * d.W * 4);
+    t.scratch = take(scan_scratch_words((uint32_t)rows) * 4);
+    if (e) *e = t;
+    return off;
+}
+
+cg_status grow_scratch(DeviceScratch* b, size_t bytes) {
+    if (b->ptr && b->bytes >= bytes) return CG_OK;
+    if (b->ptr) CG_CUDA(cudaFree(b->ptr));
+    b->ptr = nullptr;
+    b->bytes = 0;
+    CG_CUDA(cudaMalloc(&b->ptr, bytes ? bytes : 1));
+    b->bytes = bytes;
+    return CG_OK;
+}
+
+// Edge table, first half: row counts and their scan; the edge total lands
+// in w.counters->edges.
+static cg_status launch_edge_rows(const MeshDims& d, const MeshWork& w, const PlaceOptions& opt,
+                                  cudaStream_t st) {
+    if (!opt.edge_rows || !opt.edge_data) {
+        set_error("dual contouring needs edge scratch buffers");
+        return CG_EINVAL;
+    }
+    CG_TRY(grow_scratch(opt.edge_rows, edge_rows_layout(d, nullptr, nullptr)));
+    EdgeRows e;
+    edge_rows_layout(d, (char*)opt.edge_rows->ptr, &e);
+    const uint32_t rows = 3 * d.n * d.n;
+    const unsigned B = 256, G = grid_for(rows, B, 8);
+    k_edge_rows<<<G, B, 0, st>>>(w.sgn, d, e.ewoff, e.ecount);
+    CG_CHECK_LAUNCH("k_edge_rows");
+    return launch_exclusive_scan(e.ecount, e.eoff, rows, e.scratch, &w.counters->edges, st);
+}
+
+// Second half, once the host knows the edge total E: the list and the
+// per-edge crossing and gradient.
+static cg_status launch_edge_data(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
+                                  const MeshWork& w, const PlaceOptions& opt, uint32_t E,
+                                  cudaStream_t st, EdgeTable* et) {
+    CG_TRY(grow_scratch(opt.edge_data, (size_t)E * 20 + 16));
+    EdgeRows e;
+    edge_rows_layout(d, (char*)opt.edge_rows->ptr, &e);
+    float4* data = (float4*)opt.edge_data->ptr;
+    uint32_t* list = (uint32_t*)(data + E);
+    {
+        const uint32_t rows = 3 * d.n * d.n;
+        const unsigned B = 256, G = grid_for(rows, B, 8);
+        k_edge_list<<<G, B, 0, st>>>(w.sgn, d, e.eoff, e.ewoff, list);
+        CG_CHECK_LAUNCH("k_edge_list");
+    }
+    const unsigned B = 128, G = (unsigned)sm_count() * 16;
+    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+#define CG_EDGE_DATA(MODE)                                                                    \
+    if (opt.root_iters)                                                                       \
+        k_edge_data<MODE, true><<<G, B, 0, st>>>(s, pp, d, w.dists, list, w.counters, data,   \
+                                                 opt.root_iters);                             \
+    else                                                                                      \
+        k_edge_data<MODE, false><<<G, B, 0, st>>>(s, pp, d, w.dists, list, w.counters, data, 0);
+    case MODE_P8: CG_EDGE_DATA(MODE_P8) break;
+    case MODE_INT: CG_EDGE_DATA(MODE_INT) break;
+    case MODE_POLAR: CG_EDGE_DATA(MODE_POLAR) break;
+    default: CG_EDGE_DATA(MODE_SPHERE) break;
+#undef CG_EDGE_DATA
+    }
+    CG_CHECK_LAUNCH("k_edge_data");
+    et->sgn = w.sgn;
+    et->eoff = e.eoff;
+    et->ewoff = e.ewoff;
+    et->data = data;
+    return CG_OK;
 }
 
 static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                              cudaStream_t st, const PlaceOptions& opt) {
+                              cudaStream_t st, const PlaceOptions& opt,
+                              const EdgeTable& et = EdgeTable{}) {
     const PlaceParams pp = place_params(su);
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
     case MODE_P8:
-        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, opt);
+        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, opt, et);
         break;
     case MODE_INT:
-        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, opt);
+        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, opt, et);
         break;
     case MODE_POLAR:
         if (opt.analytic_normals)
-            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, opt);
+            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, opt, et);
         else
-            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, opt);
+            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, opt, et);
         break;
     default:
-        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, opt);
+        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, opt, et);
         break;
     }
     CG_CHECK_LAUNCH("k_place");
@@ -283,6 +439,15 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
                                  cudaEvent_t ev_after_vertices, bool signs_ready,
                                  const PlaceOptions& opt, const SideStream* side) {
     CG_TRY(launch_cells(d, w, st, signs_ready));
+    // Dual contouring: the edge table (its size is read back once).
+    auto edge_table = [&](EdgeTable* et) -> cg_status {
+        CG_TRY(launch_edge_rows(d, w, opt, st));
+        uint32_t E = 0;
+        CG_CUDA(cudaMemcpyAsync(&E, &w.counters->edges, sizeof E, cudaMemcpyDeviceToHost, st));
+        CG_CUDA(cudaStreamSynchronize(st));
+        return launch_edge_data(s, place_params(su), d, w, opt, E, st, et);
+    };
+    EdgeTable et{};
     if (side) {
         // The quads need only the cell table and the signs: they run on the
         // side stream while the (compute-bound) vertex placement runs here.
@@ -291,12 +456,14 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
         CG_TRY(launch_quad_count(d, w, side->stream));
         CG_TRY(launch_quad_emit(d, w, idx, icap, side->stream));
         CG_CUDA(cudaEventRecord(side->join, side->stream));
-        CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt));
+        if (opt.qef) CG_TRY(edge_table(&et));
+        CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt, et));
         if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
         CG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
         return CG_OK;
     }
-    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt));
+    if (opt.qef) CG_TRY(edge_table(&et));
+    CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt, et));
     if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
     CG_TRY(launch_quad_count(d, w, st));
     CG_TRY(launch_quad_emit(d, w, idx, icap, st));
@@ -311,6 +478,7 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
                               const PlaceOptions& opt) {
     CG_TRY(launch_cells(d, w, st, /*signs_ready=*/true));
     CG_TRY(launch_quad_count(d, w, st));
+    if (opt.qef) CG_TRY(launch_edge_rows(d, w, opt, st));
     CG_CUDA(cudaMemcpyAsync(hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaEventRecord(ev_counts, st));
     CG_CUDA(cudaEventSynchronize(ev_counts));
@@ -323,7 +491,9 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     if (ci)
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 copy_st));
-    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, opt));
+    EdgeTable et{};
+    if (opt.qef) CG_TRY(launch_edge_data(s, place_params(su), d, w, opt, hcnt->edges, st, &et));
+    CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, opt, et));
     return CG_OK;
 }
 

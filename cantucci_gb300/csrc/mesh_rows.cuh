@@ -100,6 +100,29 @@ __device__ __forceinline__ float pick8(const float (&dd)[8], uint32_t k) {
 constexpr uint64_t kEdgeFrom = 0x642054103210ull;  // 0,1,2,3, 0,1,4,5, 0,2,4,6
 constexpr uint64_t kEdgeTo = 0x753176327654ull;    // 4,5,6,7, 2,3,6,7, 1,3,5,7
 
+// Dual contouring's edge table.  Edge (a, x, y, z) joins corner (x, y, z)
+// to its +a neighbour; row r = a n^2 + x n + y holds the edges of corner
+// row (x, y) along axis a, 32 corners per word.  An edge's id is
+// eoff[r] + ewoff[r W + w] + popc(bits below z), so the edges of all cells
+// are numbered once, and table entry `id` holds (t, dDE/dp) of the edge's
+// crossing a + t (b - a).
+struct EdgeTable {
+    const uint32_t* sgn;
+    const uint32_t* eoff;   // edges before row r (3 n^2)
+    const uint32_t* ewoff;  // edges before word w within row r (3 n^2 W)
+    const float4* data;     // per edge: t, gradient
+};
+
+// Sign-change bits of the axis-a edges of corner row (x, y), word w.
+__device__ __forceinline__ uint32_t edge_bits(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                              uint32_t a, uint32_t x, uint32_t y, uint32_t w) {
+    const uint32_t row = x * d.n + y;
+    const uint32_t base = sgn[row * d.W + w];
+    if (a == 0) return x + 1 < d.n ? base ^ sgn[(row + d.n) * d.W + w] : 0u;
+    if (a == 1) return y + 1 < d.n ? base ^ sgn[(row + 1) * d.W + w] : 0u;
+    return (base ^ sign_hi(sgn, row, d.W, w)) & valid_mask(d.res, w);
+}
+
 // The reference's crossing on edge (from, to) of a cell with first corner
 // p0 (buffer.rs:187-250): the factor w = (d_from + delta) / delta, delta =
 // d_to - d_from, after the distances are oriented so that d_from < 0 (0.5
@@ -140,6 +163,45 @@ __device__ __forceinline__ void lerp_crossing(const PlaceParams& pp, float p0x, 
     cz = __fadd_rn(__fmul_rn(az, omt), __fmul_rn(bz, wgt));
 }
 
+// The DE's root on the edge a + t e, t in [0, 1], by `iters` Illinois
+// (modified regula falsi) steps from the corner distances f0 (t = 0) and f1
+// (t = 1), whose sign bits differ; NaN counts as inside, as the sign bit
+// says.  A step that leaves the bracket (NaN or degenerate) bisects.
+template <int M>
+__device__ __forceinline__ float root_on_edge(const ShapeDev& s, float ax, float ay, float az,
+                                              float ex, float ey, float ez, float f0, float f1,
+                                              uint32_t iters) {
+    const uint32_t in0 = __float_as_uint(f0) >> 31;
+    float t0 = 0.0f, t1 = 1.0f, t = 0.5f;
+    int side = 0;
+    for (uint32_t it = 0; it < iters; ++it) {
+        float tc = (t0 * f1 - t1 * f0) / (f1 - f0);
+        if (!(tc > t0 && tc < t1)) tc = 0.5f * (t0 + t1);
+        const float fc = eval<M>(s, ax + tc * ex, ay + tc * ey, az + tc * ez);
+        if ((__float_as_uint(fc) >> 31) == in0) {
+            t0 = tc;
+            f0 = fc;
+            if (side == -1) f1 *= 0.5f;
+            side = -1;
+        } else {
+            t1 = tc;
+            f1 = fc;
+            if (side == 1) f0 *= 0.5f;
+            side = 1;
+        }
+        t = tc;
+    }
+    return t;
+}
+
+// The zero of the linear interpolant of an edge's corner distances, t in
+// [0, 1] (0.5 where that is undefined).  The reference's lerp sits at 1 - t:
+// its weight d_to / (d_to - d_from) multiplies the `to` corner.
+__device__ __forceinline__ float linear_root(float f0, float f1) {
+    const float t = f0 / (f0 - f1);
+    return (t >= 0.0f && t <= 1.0f) ? t : 0.5f;
+}
+
 // Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
 // crossings, DE at the vertex and the six-sample central-difference normal.
 // With AN (polar form only) the normal is instead the normalised analytic
@@ -150,17 +212,18 @@ __device__ __forceinline__ void lerp_crossing(const PlaceParams& pp, float p0x, 
 // distances -- the refinement buffer.rs:178-186 leaves for
 // later (issue #1).  With QEF the vertex is not the crossings' centroid but
 // the dual-contouring minimiser of their tangent planes (qef.cuh; issue #2),
-// with each plane's normal from one forward-mode gradient at its crossing;
-// its crossings are the roots (ROOT) or the zeros of the linear interpolant
-// of the corner distances, not the reference's lerp points, which sit
-// mirrored about the edge midpoint.
+// from the edge table `et` (crossing and gradient per edge, built by
+// k_edge_data: roots or zeros of the linear interpolant of the corner
+// distances, not the reference's lerp points, which sit mirrored about the
+// edge midpoint); ROOT is then unused.
 // Neither changes the cell table or the index list.
 // Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
 template <int M, bool AN = false, bool ROOT = false, bool QEF = false>
 __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
                                              const MeshDims& d, const float* __restrict__ dists,
                                              uint32_t c, float* __restrict__ o,
-                                             uint32_t root_iters = 0) {
+                                             uint32_t root_iters = 0,
+                                             const EdgeTable* et = nullptr) {
     const uint32_t z = c % d.res, xy = c / d.res, y = xy % d.res, x = xy / d.res;
     float dd[8];
 #pragma unroll
@@ -190,9 +253,8 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
         sz = __fadd_rn(sz, cz);
         ++count;
     }
-    Qef q = {};
-    if constexpr (ROOT || QEF) {
-        if constexpr (ROOT) sx = sy = sz = 0.0f;
+    if constexpr (ROOT && !QEF) {
+        sx = sy = sz = 0.0f;
 #pragma unroll 1
         for (uint32_t m = xmask; m; m &= m - 1) {
             const uint32_t k = __ffs(m) - 1;
@@ -204,48 +266,37 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
             const float ex = (((to >> 2) & 1) ? pp.step[0] : 0.0f) - (((from >> 2) & 1) ? pp.step[0] : 0.0f);
             const float ey = (((to >> 1) & 1) ? pp.step[1] : 0.0f) - (((from >> 1) & 1) ? pp.step[1] : 0.0f);
             const float ez = ((to & 1) ? pp.step[2] : 0.0f) - ((from & 1) ? pp.step[2] : 0.0f);
-            float f0 = pick8(dd, from), f1 = pick8(dd, to);
-            float t;
-            if constexpr (ROOT) {
-                const uint32_t in0 = __float_as_uint(f0) >> 31;  // the sign bit: NaN counts as inside
-                float t0 = 0.0f, t1 = 1.0f;
-                int side = 0;
-                t = 0.5f;
-                for (uint32_t it = 0; it < root_iters; ++it) {
-                    float tc = (t0 * f1 - t1 * f0) / (f1 - f0);
-                    if (!(tc > t0 && tc < t1)) tc = 0.5f * (t0 + t1);  // NaN or degenerate: bisect
-                    const float fc = eval<M>(s, ax + tc * ex, ay + tc * ey, az + tc * ez);
-                    if ((__float_as_uint(fc) >> 31) == in0) {
-                        t0 = tc;
-                        f0 = fc;
-                        if (side == -1) f1 *= 0.5f;
-                        side = -1;
-                    } else {
-                        t1 = tc;
-                        f1 = fc;
-                        if (side == 1) f0 *= 0.5f;
-                        side = 1;
-                    }
-                    t = tc;
-                }
-            } else {
-                // The zero of the linear interpolant of the corner distances.
-                // (The reference's lerp above sits at 1 - t: its weight
-                // d_to / (d_to - d_from) multiplies the `to` corner.)
-                t = f0 / (f0 - f1);
-                if (!(t >= 0.0f && t <= 1.0f)) t = 0.5f;
-            }
-            const float cx = ax + t * ex, cy = ay + t * ey, cz = az + t * ez;
-            if constexpr (ROOT) {
-                sx += cx;
-                sy += cy;
-                sz += cz;
-            }
-            if constexpr (QEF) {
-                float g[4];
-                shape_gradient<M>(s, cx, cy, cz, g);
-                qef_add(q, cx - p0x, cy - p0y, cz - p0z, g[1], g[2], g[3]);
-            }
+            const float t = root_on_edge<M>(s, ax, ay, az, ex, ey, ez, pick8(dd, from),
+                                            pick8(dd, to), root_iters);
+            sx += ax + t * ex;
+            sy += ay + t * ey;
+            sz += az + t * ez;
+        }
+    }
+    Qef q = {};
+    if constexpr (QEF) {
+        // Each crossing edge's (t, gradient) from the edge table; `from` is
+        // the edge's lower corner, so the crossing is at t along +axis from
+        // it, in coordinates relative to p0.
+#pragma unroll 1
+        for (uint32_t m = xmask; m; m &= m - 1) {
+            const uint32_t k = __ffs(m) - 1;
+            const uint32_t from = (uint32_t)(kEdgeFrom >> (4 * k)) & 7u;
+            const uint32_t a = k >> 2;  // EDGES: x edges, then y, then z
+            const uint32_t cx = x + ((from >> 2) & 1), cy = y + ((from >> 1) & 1),
+                           cz = z + (from & 1);
+            const uint32_t w = cz >> 5, b = cz & 31;
+            const uint32_t r = a * d.n * d.n + cx * d.n + cy;
+            const uint32_t bits = edge_bits(et->sgn, d, a, cx, cy, w);
+            const uint32_t id = et->eoff[r] + et->ewoff[r * d.W + w] + __popc(bits & ((1u << b) - 1u));
+            const float4 e = et->data[id];
+            float rx = ((from >> 2) & 1) ? pp.step[0] : 0.0f;
+            float ry = ((from >> 1) & 1) ? pp.step[1] : 0.0f;
+            float rz = (from & 1) ? pp.step[2] : 0.0f;
+            if (a == 0) rx += e.x * pp.step[0];
+            else if (a == 1) ry += e.x * pp.step[1];
+            else rz += e.x * pp.step[2];
+            qef_add(q, rx, ry, rz, e.y, e.z, e.w);
         }
     }
     const float cf = (float)count;
