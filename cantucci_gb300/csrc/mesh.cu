@@ -195,8 +195,10 @@ __global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, M
             t = root_on_edge<M>(s, ax, ay, az, ex, ey, ez, f0, f1, root_iters);
         else
             t = linear_root(f0, f1);
+        // The crossing a + t e, one rounding per coordinate (e is 0 off the
+        // edge's axis).
         float g[4];
-        shape_gradient<M>(s, ax + t * ex, ay + t * ey, az + t * ez, g);
+        shape_gradient<M>(s, __fmaf_rn(t, ex, ax), __fmaf_rn(t, ey, ay), __fmaf_rn(t, ez, az), g);
         data[i] = make_float4(t, g[1], g[2], g[3]);
     }
 }

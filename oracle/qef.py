@@ -62,10 +62,14 @@ def crossings(dists, cells, start, step):
     with np.errstate(invalid="ignore", divide="ignore"):
         t = (f0 / (f0 - f1)).astype(f32)
     t = np.where((t >= 0) & (t <= 1), t, f32(0.5)).astype(f32)
-    a = (p0[:, None, :] + np.where(CORNER[EDGE_FROM][None] == 1, step, f32(0))).astype(f32)
+    # The edge's lower corner from its own grid coordinate, start + c * step
+    # in f32, and the crossing a + t e with one rounding per coordinate (an
+    # FMA: t e is exact in FP64).
+    corner_lo = (cells[:, None, :] + CORNER[EDGE_FROM][None]).astype(f32)
+    a = (start + (corner_lo * step).astype(f32)).astype(f32)
     e = (np.where(CORNER[EDGE_TO][None] == 1, step, f32(0))
          - np.where(CORNER[EDGE_FROM][None] == 1, step, f32(0))).astype(f32)
-    pts = (a + t[..., None] * e).astype(f32)
+    pts = (a.astype(np.float64) + t[..., None].astype(np.float64) * e.astype(np.float64)).astype(f32)
     return pts, mask, p0
 
 
