@@ -155,10 +155,37 @@ struct MbState {
     uint32_t steps, escaped;
 };
 
+// One iteration of Mandelbulb::min_distance_from's loop (mandelbulb.rs:
+// 63-75): r = |z|; false if r > bailout (escape), else dr and z advance.
+template <class O, bool P8>
+__device__ __forceinline__ bool mandelbulb_step(int32_t P, float Pf, float bailout, float px,
+                                                float py, float pz, float& zx, float& zy,
+                                                float& zz, float& dr, float& r) {
+    r = magnitude<O>(zx, zy, zz);
+    if (r > bailout) return false;
+    dr = O::add(O::mul(O::mul(powi<O>(r, P - 1), Pf), dr), 1.0f);
+    float nx, ny, nz;
+    if (on_z_axis(zx, zy)) {
+        nx = 0.0f;
+        ny = 0.0f;
+        nz = rotate_axis_z<O>(P, zx, zy, zz);
+    } else if (P8) {
+        rotate_p8<O>(zx, zy, zz, nx, ny, nz);
+    } else {
+        rotate_generic<O>(P, zx, zy, zz, nx, ny, nz);
+    }
+    zx = O::add(nx, px);
+    zy = O::add(ny, py);
+    zz = O::add(nz, pz);
+    return true;
+}
+
 // Mandelbulb::min_distance_from (mandelbulb.rs:59-79) for power P (P8 = true
 // selects the polynomial at compile time).  `r` is stale when the loop runs
-// out: it is |z| at the start of the last iteration.
-template <class O, bool P8>
+// out: it is |z| at the start of the last iteration.  FIXED > 0 is a
+// compile-time max_iters: the loop is unrolled, which drops the trip-count
+// test from every iteration (same operations, same bits).
+template <class O, bool P8, int FIXED = 0>
 __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, float bailout,
                                                float px, float py, float pz,
                                                MbState* st = nullptr) {
@@ -167,27 +194,23 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
     float r = 0.0f;
     const float Pf = (float)P;
     uint32_t steps = 0, esc = 0;
-    for (uint32_t i = 0; i < max_iters; ++i) {
-        r = magnitude<O>(zx, zy, zz);
-        if (r > bailout) {
-            esc = 1;
-            break;
+    if constexpr (FIXED > 0) {
+#pragma unroll
+        for (int i = 0; i < FIXED; ++i) {
+            if (!mandelbulb_step<O, P8>(P, Pf, bailout, px, py, pz, zx, zy, zz, dr, r)) {
+                esc = 1;
+                break;
+            }
+            ++steps;
         }
-        dr = O::add(O::mul(O::mul(powi<O>(r, P - 1), Pf), dr), 1.0f);
-        float nx, ny, nz;
-        if (on_z_axis(zx, zy)) {
-            nx = 0.0f;
-            ny = 0.0f;
-            nz = rotate_axis_z<O>(P, zx, zy, zz);
-        } else if (P8) {
-            rotate_p8<O>(zx, zy, zz, nx, ny, nz);
-        } else {
-            rotate_generic<O>(P, zx, zy, zz, nx, ny, nz);
+    } else {
+        for (uint32_t i = 0; i < max_iters; ++i) {
+            if (!mandelbulb_step<O, P8>(P, Pf, bailout, px, py, pz, zx, zy, zz, dr, r)) {
+                esc = 1;
+                break;
+            }
+            ++steps;
         }
-        zx = O::add(nx, px);
-        zy = O::add(ny, py);
-        zz = O::add(nz, pz);
-        ++steps;
     }
     if (st) {
         st->r = r;
@@ -592,12 +615,17 @@ enum Mode {
     MODE_SPHERE = 3,
     MODE_P8_FAST = 4,
     MODE_INT_POLY = 5,
-    MODE_POLAR_FAST = 6
+    MODE_POLAR_FAST = 6,
+    // MODE_P8 with max_iters == 15 (the reference's default), the loop
+    // unrolled at compile time; chosen at launch by the grid, point and
+    // placement kernels (p8_mode), never returned by mode_of.
+    MODE_P8_IT15 = 7
 };
 
 template <int M>
 __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
     if (M == MODE_P8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
+    if (M == MODE_P8_IT15) return mandelbulb_de<Exact, true, 15>(8, 15, s.bailout, x, y, z);
     if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
     if (M == MODE_POLAR) return polar_de(s, x, y, z);
     if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
@@ -606,6 +634,9 @@ __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float
     return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
 }
 
+
+// MODE_P8 or, for max_iters 15, its unrolled twin.
+__host__ __forceinline__ bool p8_unrolled(const ShapeDev& s) { return s.max_iters == 15; }
 
 // Kernel mode of a shape (integer P=8 takes the polynomial).
 __host__ __device__ __forceinline__ int mode_of(const ShapeDev& s, uint32_t numerics) {

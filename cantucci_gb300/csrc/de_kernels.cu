@@ -217,7 +217,10 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
     if (n == 0) return CG_OK;
     const unsigned B = 256, G = grid_for(n, B, 16);
     switch (mode_of(s, numerics)) {
-    case MODE_P8: k_de_points<MODE_P8><<<G, B, 0, st>>>(s, pts, n, out); break;
+    case MODE_P8:
+        if (p8_unrolled(s)) k_de_points<MODE_P8_IT15><<<G, B, 0, st>>>(s, pts, n, out);
+        else k_de_points<MODE_P8><<<G, B, 0, st>>>(s, pts, n, out);
+        break;
     case MODE_INT: k_de_points<MODE_INT><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_POLAR: k_de_points<MODE_POLAR><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_SPHERE: k_de_points<MODE_SPHERE><<<G, B, 0, st>>>(s, pts, n, out); break;
@@ -289,7 +292,7 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
     const unsigned B = 256;
     int k = g_de_grid_kernel;
     if (k == DE_GRID_AUTO) k = g.n >= 33 ? DE_GRID_BRICK : DE_GRID_LINEAR;
-    if (k == DE_GRID_PACKED && M == MODE_P8) {
+    if (k == DE_GRID_PACKED && (M == MODE_P8 || M == MODE_P8_IT15)) {
         const uint64_t b4 = (g.n + 3) >> 2;
         k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
     } else if (k != DE_GRID_LINEAR) {
@@ -304,7 +307,10 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
                          cudaStream_t st, uint32_t* sgn, uint32_t W) {
     switch (mode_of(s, numerics)) {
-    case MODE_P8: launch_grid_mode<MODE_P8>(s, g, out, sgn, W, st); break;
+    case MODE_P8:
+        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_IT15>(s, g, out, sgn, W, st);
+        else launch_grid_mode<MODE_P8>(s, g, out, sgn, W, st);
+        break;
     case MODE_INT: launch_grid_mode<MODE_INT>(s, g, out, sgn, W, st); break;
     case MODE_POLAR: launch_grid_mode<MODE_POLAR>(s, g, out, sgn, W, st); break;
     case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st); break;

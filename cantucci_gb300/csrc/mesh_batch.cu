@@ -574,7 +574,10 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     CG_CUDA(cudaMemsetAsync(b->tot, 0, sizeof(BatchTotals), st));
     CG_CUDA(cudaMemsetAsync(b->sgn, 0, b->sgn_words * 4, st));
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
-    case MODE_P8: CG_TRY(launch_batch_de<MODE_P8>(b, s, st)); break;
+    case MODE_P8:
+        if (p8_unrolled(s)) CG_TRY(launch_batch_de<MODE_P8_IT15>(b, s, st));
+        else CG_TRY(launch_batch_de<MODE_P8>(b, s, st));
+        break;
     case MODE_INT: CG_TRY(launch_batch_de<MODE_INT>(b, s, st)); break;
     case MODE_POLAR: CG_TRY(launch_batch_de<MODE_POLAR>(b, s, st)); break;
     default: CG_TRY(launch_batch_de<MODE_SPHERE>(b, s, st)); break;
@@ -603,7 +606,10 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     CG_CHECK_LAUNCH("k_batch_quad_emit");
     if (b->side) CG_CUDA(cudaEventRecord(b->join, b->side));
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
-    case MODE_P8: CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st)); break;
+    case MODE_P8:
+        if (p8_unrolled(s)) CG_TRY(launch_batch_place<MODE_P8_IT15>(b, s, vertices, vertex_cap, st));
+        else CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st));
+        break;
     case MODE_INT: CG_TRY(launch_batch_place<MODE_INT>(b, s, vertices, vertex_cap, st)); break;
     case MODE_POLAR: CG_TRY(launch_batch_place<MODE_POLAR>(b, s, vertices, vertex_cap, st)); break;
     default: CG_TRY(launch_batch_place<MODE_SPHERE>(b, s, vertices, vertex_cap, st)); break;

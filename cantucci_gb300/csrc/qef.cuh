@@ -131,7 +131,7 @@ __device__ __forceinline__ void shape_gradient(const ShapeDev& s, float x, float
         g[1] = dx * inv;
         g[2] = dy * inv;
         g[3] = dz * inv;
-    } else if constexpr (M == MODE_P8 || M == MODE_P8_FAST) {
+    } else if constexpr (M == MODE_P8 || M == MODE_P8_IT15 || M == MODE_P8_FAST) {
         p8_de_gradient(s.max_iters, s.bailout, x, y, z, g);
     } else {
         float o[5];
