@@ -617,8 +617,8 @@ enum Mode {
     MODE_INT_POLY = 5,
     MODE_POLAR_FAST = 6,
     // MODE_P8 with max_iters == 15 (the reference's default), the loop
-    // unrolled at compile time; chosen at launch by the grid, point and
-    // placement kernels (p8_mode), never returned by mode_of.
+    // unrolled at compile time; chosen at launch (p8_unrolled) by the grid
+    // and point kernels, never returned by mode_of.
     MODE_P8_IT15 = 7
 };
 

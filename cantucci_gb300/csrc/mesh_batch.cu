@@ -607,8 +607,7 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     if (b->side) CG_CUDA(cudaEventRecord(b->join, b->side));
     switch (mode_of(s, CG_NUMERICS_EXACT)) {
     case MODE_P8:
-        if (p8_unrolled(s)) CG_TRY(launch_batch_place<MODE_P8_IT15>(b, s, vertices, vertex_cap, st));
-        else CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st));
+        CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st));  // rolled, as k_place
         break;
     case MODE_INT: CG_TRY(launch_batch_place<MODE_INT>(b, s, vertices, vertex_cap, st)); break;
     case MODE_POLAR: CG_TRY(launch_batch_place<MODE_POLAR>(b, s, vertices, vertex_cap, st)); break;
