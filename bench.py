@@ -657,6 +657,43 @@ def extra_dual_contouring(dev, res=RES):
     return out
 
 
+def extra_fast_numerics(dev, res=RES):
+    """The 513^3 span meshed with the exact estimator (the reference's bits)
+    and with CG_NUMERICS_FAST (FMA-contracted P=8 polynomial, approximate
+    division and square roots): mesh time, counts and the fraction of
+    corners whose sign agrees with the exact grid."""
+    import torch
+    import cantucci_gb300 as cg
+    from cantucci_gb300 import workloads as W
+    span = cg.Span(*W.SPAN_C1)
+    shape = cg.Mandelbulb(**SHAPE)
+    vcap, icap = res ** 3 // 16, 18 * res ** 3 // 16
+    v = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
+    i = torch.empty(icap, dtype=torch.int32, device=dev)
+    out = {"workload": "Mandelbulb P=8 max_iters 15, %d^3 corners" % (res + 1)}
+    signs = {}
+    m = cg.Mesher(dev)
+    try:
+        for mode in ("exact", "fast"):
+            m.set_numerics(mode)
+            m.generate_device(span, shape, res, v, i, strict=False)
+            best = None
+            for _ in range(3):
+                nv, ni, tm = m.generate_device(span, shape, res, v, i, strict=False)
+                ms = tm.first_ms + tm.second_ms + tm.third_ms
+                if best is None or ms < best[0]:
+                    best = (ms, tm.first_ms, tm.second_ms)
+            signs[mode] = torch.signbit(m.last_dists())
+            out[mode] = {"mesh_ms": best[0], "step1_ms": best[1], "step2_ms": best[2],
+                         "corners_per_s": (res + 1) ** 3 / (best[0] * 1e-3),
+                         "vertices": nv, "quads": ni // 6}
+    finally:
+        m.close()
+    out["sign_agreement"] = float((signs["exact"] == signs["fast"]).float().mean())
+    out["speedup"] = out["exact"]["mesh_ms"] / out["fast"]["mesh_ms"]
+    return out
+
+
 def run_extras(args, dev):
     """The other configurations.  The oracle runs only in CPU legs (the CPU
     builder's timing and the accuracy checks against FP64), which
@@ -670,6 +707,7 @@ def run_extras(args, dev):
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
             ("root_crossings", lambda: extra_root_crossings(dev)),
             ("dual_contouring", lambda: extra_dual_contouring(dev)),
+            ("fast_numerics", lambda: extra_fast_numerics(dev)),
             ("lod", lambda: extra_lod(dev, cpu)),
             ("depth_fit", lambda: extra_depth_fit(dev, args.fit_steps))]
     if cpu:

@@ -105,6 +105,7 @@ SIGNATURES = [
     ("cg_mesher_set_normals", _i32, [_vp, _u32]),
     ("cg_mesher_set_crossings", _i32, [_vp, _u32, _u32]),
     ("cg_mesher_set_placement", _i32, [_vp, _u32]),
+    ("cg_mesher_set_numerics", _i32, [_vp, _u32]),
     ("cg_generate_for_box", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,
                                    C.POINTER(_u64), C.POINTER(_u64), _tmp]),
     ("cg_generate_for_box_device", _i32, [_vp, _spp, _shp, _u32, _vp, _u64, _vp, _u64,

@@ -294,6 +294,13 @@ class Mesher:
         modes = {"centroid": _ffi.CG_PLACEMENT_CENTROID, "qef": _ffi.CG_PLACEMENT_QEF}
         check(self._lib.cg_mesher_set_placement(self.handle, modes[mode]))
 
+    def set_numerics(self, mode: str):
+        """"exact": the reference's bits (default); "fast": the fast estimator
+        for the whole mesh (cells near the surface may differ; default
+        normals, crossings and placement only)."""
+        modes = {"exact": _ffi.CG_NUMERICS_EXACT, "fast": _ffi.CG_NUMERICS_FAST}
+        check(self._lib.cg_mesher_set_numerics(self.handle, modes[mode]))
+
     def generate(self, span: Span, shape: Shape, resolution: int, vertex_cap=None,
                  index_cap=None, vertices=None, indices=None, strict: bool = True):
         """Mesh into host numpy arrays (pinned torch tensors also accepted).

@@ -156,6 +156,7 @@ struct cg_mesher {
     uint32_t normals = CG_NORMALS_FD;
     uint32_t root_iters = 0;  // CG_CROSSINGS_LERP
     uint32_t placement = CG_PLACEMENT_CENTROID;
+    uint32_t numerics = CG_NUMERICS_EXACT;
     DeviceScratch edge_rows, edge_data;  // dual contouring's edge table
     uint32_t last_res = 0;
     MeshWork last_w{};
@@ -169,6 +170,7 @@ PlaceOptions place_options(cg_mesher* m) {
     o.analytic_normals = m->normals == CG_NORMALS_ADJOINT;
     o.root_iters = m->root_iters;
     o.qef = m->placement == CG_PLACEMENT_QEF;
+    o.numerics = m->numerics;
     o.edge_rows = &m->edge_rows;
     o.edge_data = &m->edge_data;
     return o;
@@ -216,7 +218,7 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     cudaStream_t st = m->stream;
     CG_CUDA(cudaEventRecord(m->ev[0], st));
     CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
-    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
+    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, m->numerics, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     const SideStream side = {m->copy_stream, m->fork, m->join};
     CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
@@ -276,7 +278,7 @@ cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* sh
     cudaStream_t st = m->stream;
     CG_CUDA(cudaEventRecord(m->ev[0], st));
     CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
-    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, CG_NUMERICS_EXACT, st, w.sgn, d.W));
+    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, m->numerics, st, w.sgn, d.W));
     CG_CUDA(cudaEventRecord(m->ev[1], st));
     CG_TRY(launch_mesh_to_host(s, su, d, w, hverts_dev, vcap, m->didx, hidx, idev, st,
                                m->copy_stream, m->ev[2], m->ev[3], m->hcnt, place_options(m)));
@@ -446,6 +448,16 @@ cg_status cg_mesher_set_crossings(cg_mesher* m, uint32_t crossings, uint32_t ite
     }
     std::lock_guard<std::mutex> lk(m->mu);
     m->root_iters = crossings == CG_CROSSINGS_ROOT ? iters : 0;
+    return CG_OK;
+}
+
+cg_status cg_mesher_set_numerics(cg_mesher* m, uint32_t numerics) {
+    if (!m || numerics > CG_NUMERICS_FAST) {
+        set_error("numerics: CG_NUMERICS_EXACT or CG_NUMERICS_FAST");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(m->mu);
+    m->numerics = numerics;
     return CG_OK;
 }
 

@@ -105,6 +105,7 @@ struct PlaceOptions {
     bool analytic_normals = false;
     uint32_t root_iters = 0;
     bool qef = false;
+    uint32_t numerics = CG_NUMERICS_EXACT;  // FAST: with none of the options above
     DeviceScratch* edge_rows = nullptr;
     DeviceScratch* edge_data = nullptr;
 };

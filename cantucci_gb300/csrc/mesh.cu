@@ -365,12 +365,31 @@ static cg_status launch_edge_data(const ShapeDev& s, const PlaceParams& pp, cons
     return CG_OK;
 }
 
+// The fast estimators (CG_NUMERICS_FAST) with the reference's placement.
+template <int M>
+static void launch_place_plain(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
+                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                               cudaStream_t st) {
+    const unsigned B = 128;
+    const unsigned G = (unsigned)sm_count() * 16;
+    k_place<M, false, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
+                                                     verts, vcap, 0, EdgeTable{});
+}
+
 static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                               cudaStream_t st, const PlaceOptions& opt,
                               const EdgeTable& et = EdgeTable{}) {
     const PlaceParams pp = place_params(su);
-    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    if (opt.numerics == CG_NUMERICS_FAST &&
+        (opt.analytic_normals || opt.root_iters || opt.qef)) {
+        set_error("fast numerics mesh with the default placement only");
+        return CG_EINVAL;
+    }
+    switch (mode_of(s, opt.numerics)) {
+    case MODE_P8_FAST: launch_place_plain<MODE_P8_FAST>(s, pp, d, w, verts, vcap, st); break;
+    case MODE_INT_POLY: launch_place_plain<MODE_INT_POLY>(s, pp, d, w, verts, vcap, st); break;
+    case MODE_POLAR_FAST: launch_place_plain<MODE_POLAR_FAST>(s, pp, d, w, verts, vcap, st); break;
     case MODE_P8:
         // (the rolled loop: with seven estimator calls per vertex the
         // unrolled one measured slower here)

@@ -175,6 +175,13 @@ cg_status cg_mesher_set_crossings(cg_mesher* mesher, uint32_t crossings, uint32_
  * table and index list are unchanged; the DE and normal are evaluated at
  * the new position.  Any shape. */
 cg_status cg_mesher_set_placement(cg_mesher* mesher, uint32_t placement);
+/* Select the estimator's numerics for the whole mesh (CG_NUMERICS_EXACT
+ * default: the reference's bits).  CG_NUMERICS_FAST meshes with the fast
+ * estimator (see the enum): the corner signs near the surface, and so the
+ * cell set, may differ from the reference's.  Only with the default
+ * normals, crossings and placement; a mesh with another option set fails
+ * with CG_EINVAL. */
+cg_status cg_mesher_set_numerics(cg_mesher* mesher, uint32_t numerics);
 
 /* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.
  * Writes min(count, cap) items; if a count exceeds its capacity the call

@@ -184,6 +184,8 @@ public:
     }
     // CG_PLACEMENT_CENTROID (the reference's) or CG_PLACEMENT_QEF (dual contouring).
     void set_placement(uint32_t placement) { check(cg_mesher_set_placement(m_, placement)); }
+    // CG_NUMERICS_EXACT (the reference's bits) or CG_NUMERICS_FAST.
+    void set_numerics(uint32_t numerics) { check(cg_mesher_set_numerics(m_, numerics)); }
 
     static Mesher& for_this_thread() {
         thread_local Mesher m(0);

@@ -374,3 +374,40 @@ def test_max_resolution_span(cg):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     finally:
         m.close()
+
+
+@pytest.mark.parametrize("kind", ["p8", "p6", "polar"])
+def test_fast_numerics_mesh(cg, kind):
+    """CG_NUMERICS_FAST for a whole mesh: the corner signs agree with the
+    exact grid almost everywhere (>= 99.9%), the vertex and quad counts stay
+    within 1% of the reference's, every index names a vertex, every vertex
+    lies in its cell; fast numerics together with another placement option
+    is refused."""
+    from oracle import qef
+    s = {"p8": cg.Mandelbulb(8, 15, 2.5), "p6": cg.Mandelbulb(6, 12, 2.5),
+         "polar": cg.MandelbulbPolar(8.3, 15, 2.5, (0.2, 0.1, 0.0))}[kind]
+    span = cg.Span(*W.SPAN_C1)
+    res = 128
+    m = cg.Mesher(0)
+    try:
+        v0, i0, nv0, ni0, _ = m.generate(span, s, res, strict=False)
+        d0 = m.last_dists().cpu().numpy()
+        m.set_numerics("fast")
+        v1, i1, nv1, ni1, _ = m.generate(span, s, res, strict=False)
+        d1 = m.last_dists().cpu().numpy()
+        pts = m.last_points().cpu().numpy()
+        m.set_placement("qef")
+        with pytest.raises(cg.CantucciError):
+            m.generate(span, s, 16)
+    finally:
+        m.close()
+    assert np.mean(np.signbit(d0) == np.signbit(d1)) >= 0.999
+    assert abs(nv1 - nv0) <= 0.01 * nv0 and abs(ni1 - ni0) <= 0.01 * ni0
+    assert ni1 > 0 and int(i1[:ni1].max()) < nv1
+    b = as7(v1[:nv1])
+    cells = np.argwhere(pts != 0xFFFFFFFF)
+    order = pts[cells[:, 0], cells[:, 1], cells[:, 2]].astype(np.int64)
+    start, step = qef.span_setup(np.array(W.SPAN_C1), res)
+    lo = (start + cells.astype(np.float32) * step).astype(np.float32)
+    ok = np.all((b[order, :3] >= lo - 1e-6) & (b[order, :3] <= lo + step + 1e-6), axis=1)
+    assert ok.all()
