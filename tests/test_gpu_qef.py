@@ -192,3 +192,46 @@ def test_placement_rejects_unknown_mode(cg):
         assert lib.cg_mesher_set_placement(m.handle, 1) == 0
     finally:
         m.close()
+
+
+@pytest.mark.parametrize("res", [2, 4, 8])
+def test_qef_small_resolutions(cg, res):
+    """The smallest spans (res 2 is the least the reference accepts): the
+    same topology as the centroid mesh and every vertex inside its cell."""
+    from oracle import qef
+    s = cg.Sphere((0.1, -0.05, 0.02), 0.9)
+    span = cg.Span(*W.SPAN_C1)
+    m = cg.Mesher(0)
+    try:
+        v0, i0, nv0, ni0, _ = m.generate(span, s, res)
+        m.set_placement("qef")
+        v1, i1, nv1, ni1, _ = m.generate(span, s, res)
+        pts = m.last_points().cpu().numpy()
+    finally:
+        m.close()
+    assert (nv0, ni0) == (nv1, ni1) and nv0 > 0
+    assert np.array_equal(i0[:ni0], i1[:ni1])
+    b = as7(v1[:nv1])
+    cells = np.argwhere(pts != 0xFFFFFFFF)
+    order = pts[cells[:, 0], cells[:, 1], cells[:, 2]].astype(np.int64)
+    start, step = qef.span_setup(np.array(W.SPAN_C1), res)
+    lo = (start + cells.astype(np.float32) * step).astype(np.float32)
+    assert np.all((b[order, :3] >= lo) & (b[order, :3] <= (lo + step).astype(np.float32)))
+
+
+def test_qef_empty_span(cg):
+    """A span the surface does not cross: no vertices, no quads, no edges,
+    through both the device and the pinned-host pipelines."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span((1.5, 1.5, 1.5), (1.9, 1.9, 1.9))
+    m = cg.Mesher(0)
+    try:
+        m.set_placement("qef")
+        _, _, nv, ni, _ = m.generate(span, s, 32)
+        hv = torch.empty((1024, 7), dtype=torch.float32).pin_memory()
+        hi = torch.empty(4096, dtype=torch.int32).pin_memory()
+        _, _, nv2, ni2, _ = m.generate(span, s, 32, vertices=hv, indices=hi)
+    finally:
+        m.close()
+    assert (nv, ni) == (0, 0) and (nv2, ni2) == (0, 0)
