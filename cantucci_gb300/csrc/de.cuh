@@ -446,31 +446,45 @@ __device__ __forceinline__ float fast_sqrt(float x) {
     return x > 0.0f ? x * rsqrtf(x) : 0.0f;
 }
 
+__device__ __forceinline__ bool p8_fast_step(float bailout, float px, float py, float pz,
+                                             float& zx, float& zy, float& zz, float& dr,
+                                             float& r) {
+    const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
+    r = fast_sqrt(r2);
+    if (r > bailout) return false;
+    const float rr2 = r * r, rr4 = rr2 * rr2;
+    dr = fmaf(rr4 * rr2 * r * 8.0f, dr, 1.0f);
+    const float x = zx, y = zy, z = zz;
+    const float x2 = x * x, y2 = y * y, z2 = z * z;
+    const float y4 = y2 * y2;
+    const float rxy2 = x2 + y2;
+    const float rxy4 = rxy2 * rxy2;
+    // num = z8 - 28 z6 rxy2 + 70 z4 rxy4 - 28 z2 rxy6 (Horner in z2)
+    const float num = fmaf(fmaf(fmaf(z2 - 28.0f * rxy2, z2, 70.0f * rxy4), z2,
+                                -28.0f * rxy4 * rxy2), z2, 0.0f);
+    const float a = 1.0f + __fdividef(num, rxy4 * rxy4);
+    const float X = fmaf(fmaf(fmaf(x2 - 28.0f * y2, x2, 70.0f * y4), x2, -28.0f * y4 * y2),
+                         x2, -y4 * y4);
+    const float Y = fmaf(fmaf(x2 - 7.0f * y2, x2, 7.0f * y4), x2, -y4 * y2);
+    const float Z = fmaf(z2 - 6.0f * rxy2, z2, rxy4);
+    zx = fmaf(a, X, px);
+    zy = fmaf(8.0f * a * x * y, Y, py);
+    zz = fmaf(8.0f * z * fast_sqrt(rxy2) * (z2 - rxy2), Z, pz);
+    return true;
+}
+
+// FIXED > 0: a compile-time max_iters, the loop unrolled.
+template <int FIXED = 0>
 __device__ __forceinline__ float mandelbulb_p8_fast(uint32_t max_iters, float bailout, float px,
                                                     float py, float pz) {
     float zx = px, zy = py, zz = pz, dr = 1.0f, r = 0.0f;
-    for (uint32_t i = 0; i < max_iters; ++i) {
-        const float r2 = fmaf(zx, zx, fmaf(zy, zy, zz * zz));
-        r = fast_sqrt(r2);
-        if (r > bailout) break;
-        const float rr2 = r * r, rr4 = rr2 * rr2;
-        dr = fmaf(rr4 * rr2 * r * 8.0f, dr, 1.0f);
-        const float x = zx, y = zy, z = zz;
-        const float x2 = x * x, y2 = y * y, z2 = z * z;
-        const float y4 = y2 * y2;
-        const float rxy2 = x2 + y2;
-        const float rxy4 = rxy2 * rxy2;
-        // num = z8 - 28 z6 rxy2 + 70 z4 rxy4 - 28 z2 rxy6 (Horner in z2)
-        const float num = fmaf(fmaf(fmaf(z2 - 28.0f * rxy2, z2, 70.0f * rxy4), z2,
-                                    -28.0f * rxy4 * rxy2), z2, 0.0f);
-        const float a = 1.0f + __fdividef(num, rxy4 * rxy4);
-        const float X = fmaf(fmaf(fmaf(x2 - 28.0f * y2, x2, 70.0f * y4), x2, -28.0f * y4 * y2),
-                             x2, -y4 * y4);
-        const float Y = fmaf(fmaf(x2 - 7.0f * y2, x2, 7.0f * y4), x2, -y4 * y2);
-        const float Z = fmaf(z2 - 6.0f * rxy2, z2, rxy4);
-        zx = fmaf(a, X, px);
-        zy = fmaf(8.0f * a * x * y, Y, py);
-        zz = fmaf(8.0f * z * fast_sqrt(rxy2) * (z2 - rxy2), Z, pz);
+    if constexpr (FIXED > 0) {
+#pragma unroll
+        for (int i = 0; i < FIXED; ++i)
+            if (!p8_fast_step(bailout, px, py, pz, zx, zy, zz, dr, r)) break;
+    } else {
+        for (uint32_t i = 0; i < max_iters; ++i)
+            if (!p8_fast_step(bailout, px, py, pz, zx, zy, zz, dr, r)) break;
     }
     return x86_nan(__fdividef(0.5f * __logf(r) * r, dr));
 }
@@ -619,7 +633,8 @@ enum Mode {
     // MODE_P8 with max_iters == 15 (the reference's default), the loop
     // unrolled at compile time; chosen at launch (p8_unrolled) by the grid
     // and point kernels, never returned by mode_of.
-    MODE_P8_IT15 = 7
+    MODE_P8_IT15 = 7,
+    MODE_P8_FAST_IT15 = 8  // MODE_P8_FAST likewise
 };
 
 template <int M>
@@ -631,11 +646,12 @@ __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float
     if (M == MODE_SPHERE) return sphere_de(s, x, y, z);
     if (M == MODE_INT_POLY) return mandelbulb_int_poly(s.power, s.max_iters, s.bailout, x, y, z);
     if (M == MODE_POLAR_FAST) return polar_de_fast(s, x, y, z);
+    if (M == MODE_P8_FAST_IT15) return mandelbulb_p8_fast<15>(15, s.bailout, x, y, z);
     return mandelbulb_p8_fast(s.max_iters, s.bailout, x, y, z);
 }
 
 
-// MODE_P8 or, for max_iters 15, its unrolled twin.
+// MODE_P8 / MODE_P8_FAST or, for max_iters 15, their unrolled twins.
 __host__ __forceinline__ bool p8_unrolled(const ShapeDev& s) { return s.max_iters == 15; }
 
 // Kernel mode of a shape (integer P=8 takes the polynomial).

@@ -226,7 +226,10 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
     case MODE_SPHERE: k_de_points<MODE_SPHERE><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_INT_POLY: k_de_points<MODE_INT_POLY><<<G, B, 0, st>>>(s, pts, n, out); break;
     case MODE_POLAR_FAST: k_de_points<MODE_POLAR_FAST><<<G, B, 0, st>>>(s, pts, n, out); break;
-    default: k_de_points<MODE_P8_FAST><<<G, B, 0, st>>>(s, pts, n, out); break;
+    default:
+        if (p8_unrolled(s)) k_de_points<MODE_P8_FAST_IT15><<<G, B, 0, st>>>(s, pts, n, out);
+        else k_de_points<MODE_P8_FAST><<<G, B, 0, st>>>(s, pts, n, out);
+        break;
     }
     CG_CHECK_LAUNCH("k_de_points");
     return CG_OK;
@@ -316,7 +319,10 @@ cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32
     case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st); break;
     case MODE_INT_POLY: launch_grid_mode<MODE_INT_POLY>(s, g, out, sgn, W, st); break;
     case MODE_POLAR_FAST: launch_grid_mode<MODE_POLAR_FAST>(s, g, out, sgn, W, st); break;
-    default: launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st); break;
+    default:
+        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_FAST_IT15>(s, g, out, sgn, W, st);
+        else launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st);
+        break;
     }
     CG_CHECK_LAUNCH("k_de_grid");
     return CG_OK;
