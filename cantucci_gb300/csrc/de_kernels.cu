@@ -58,11 +58,15 @@ __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* _
     }
 }
 
-// Large grids: each warp evaluates a 2x4x4 brick of corners (x, y, z), which
+// Large grids: each warp evaluates 2x4x4 bricks of corners (x, y, z), which
 // keeps the escape counts of a warp's lanes close (89% lane efficiency on the
-// 513^3 span vs 75% for 32 corners along z).  With `sgn`, the four z-lanes of
-// each (x, y) pair OR their sign bits together and one lane sets them in the
-// sign word with atomicOr (sgn must be zeroed first).
+// 513^3 span vs 75% for 32 corners along z).  A warp owns the run of up to 8
+// bricks along z (bz = 8 gz .. 8 gz + 7): for each of its 8 (x, y) rows that
+// is 32 consecutive distances (whole 128-byte lines) and, with `sgn`, exactly
+// sign word gz.  One ballot per brick gives the signs; the z-lane-0 thread
+// of each row collects its row's 4 bits per brick and stores the finished
+// word once: no atomics, and every word of sgn is written (padding bits
+// beyond the last corner are 0).
 template <int M>
 __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
                                                        float* __restrict__ out,
@@ -72,29 +76,34 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
     const uint32_t BX = (n + 1) >> 1, BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
-    // Brick (bx, by, bz) of this warp, advanced by the grid stride written in
-    // the same mixed radix, so the loop does no integer division.
-    const uint32_t b0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t bz = b0 % BZ, by = (b0 / BZ) % BY, bx = b0 / (BZ * BY);
-    const uint32_t sz = nwarps % BZ, sy = (nwarps / BZ) % BY, sx = nwarps / (BZ * BY);
+    // Unit (bx, by, gz), advanced by the grid stride in the same mixed radix.
+    const uint32_t u0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t gz = u0 % W, by = (u0 / W) % BY, bx = u0 / (W * BY);
+    const uint32_t sz = nwarps % W, sy = (nwarps / W) % BY, sx = nwarps / (W * BY);
     for (; bx < BX;) {
-        const uint32_t x = 2 * bx + dx, y = 4 * by + dy, z = 4 * bz + dz;
-        const bool active = x < n && y < n && z < n;
-        uint32_t bit = 0;
-        if (active) {
-            const float d = eval<M>(s, grid_coord(g, 0, x), grid_coord(g, 1, y), grid_coord(g, 2, z));
-            out[((size_t)x * n + y) * n + z] = d;
-            bit = (__float_as_uint(d) >> 31) ? 0u : (1u << (z & 31));
+        const uint32_t x = 2 * bx + dx, y = 4 * by + dy;
+        const bool row_ok = x < n && y < n;
+        const float px = grid_coord(g, 0, x), py = grid_coord(g, 1, y);
+        const uint32_t bz_end = min(8 * gz + 8, BZ);
+        uint32_t word = 0;
+        for (uint32_t bz = 8 * gz; bz < bz_end; ++bz) {
+            const uint32_t z = 4 * bz + dz;
+            bool pos = false;
+            if (row_ok && z < n) {
+                const float d = eval<M>(s, px, py, grid_coord(g, 2, z));
+                out[((size_t)x * n + y) * n + z] = d;
+                pos = (__float_as_uint(d) >> 31) == 0u;
+            }
+            if (sgn) {
+                const uint32_t b = __ballot_sync(0xFFFFFFFFu, pos);
+                word |= ((b >> (lane & ~3u)) & 0xFu) << ((4 * bz) & 31);
+            }
         }
-        if (sgn) {
-            bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 1);
-            bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 2);
-            if (dz == 0 && bit) atomicOr(&sgn[(x * n + y) * W + (z >> 5)], bit);
-        }
-        bz += sz;
+        if (sgn && dz == 0 && row_ok) sgn[(x * n + y) * W + gz] = word;
+        gz += sz;
         uint32_t carry = 0;
-        if (bz >= BZ) {
-            bz -= BZ;
+        if (gz >= W) {
+            gz -= W;
             carry = 1;
         }
         by += sy + carry;
@@ -237,7 +246,9 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
 
 // P=8 exact, two corners per thread with packed f32x2 instructions: each
 // warp evaluates a 4x4x4 brick, lane (dx, dy, dz) taking corners (x, y, z)
-// and (x + 2, y, z).  Sign words as in k_de_grid_brick.
+// and (x + 2, y, z).  With `sgn` the four z-lanes of each (x, y) row OR their
+// sign bits with two shuffles and one lane sets them with atomicOr (sgn must
+// be zeroed first).
 __global__ void __launch_bounds__(256) k_de_grid_p8x2(ShapeDev s, GridDev g,
                                                       float* __restrict__ out,
                                                       uint32_t* __restrict__ sgn, uint32_t W) {
@@ -299,8 +310,10 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
         const uint64_t b4 = (g.n + 3) >> 2;
         k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
     } else if (k != DE_GRID_LINEAR) {
-        const uint64_t bricks = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2) * ((g.n + 3) >> 2);
-        k_de_grid_brick<M><<<grid_for(bricks * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+        // W words per row; without sign words the same (bx, by, gz) walk.
+        const uint32_t Wz = sgn ? W : (g.n + 31) / 32;
+        const uint64_t units = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2) * Wz;
+        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, Wz);
     } else {
         const uint64_t total = (uint64_t)g.n * g.n * g.n;
         k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W);
