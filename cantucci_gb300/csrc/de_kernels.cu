@@ -60,33 +60,37 @@ __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* _
 
 // Large grids: each warp evaluates 2x4x4 bricks of corners (x, y, z), which
 // keeps the escape counts of a warp's lanes close (89% lane efficiency on the
-// 513^3 span vs 75% for 32 corners along z).  A warp owns the run of up to 8
-// bricks along z (bz = 8 gz .. 8 gz + 7): for each of its 8 (x, y) rows that
-// is 32 consecutive distances (whole 128-byte lines) and, with `sgn`, exactly
-// sign word gz.  One ballot per brick gives the signs; the z-lane-0 thread
-// of each row collects its row's 4 bits per brick and stores the finished
-// word once: no atomics, and every word of sgn is written (padding bits
-// beyond the last corner are 0).
+// 513^3 span vs 75% for 32 corners along z).  A work unit is a run of
+// `group` bricks along z.  With group 8 (grids with work for several waves)
+// the unit covers 32 consecutive distances of each of its 8 (x, y) rows
+// (whole 128-byte lines) and, with `sgn`, exactly one sign word per row:
+// one ballot per brick gives the signs, the z-lane-0 thread of each row
+// collects its row's 4 bits per brick and stores the finished word once (no
+// atomics; every word is written, padding bits 0).  With group 1 (smaller
+// grids, where 8-brick units would leave SMs idle) each brick's 4 bits go
+// into the word with atomicOr (sgn zeroed first).
 template <int M>
 __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
                                                        float* __restrict__ out,
-                                                       uint32_t* __restrict__ sgn, uint32_t W) {
+                                                       uint32_t* __restrict__ sgn, uint32_t W,
+                                                       uint32_t group) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t n = g.n;
     const uint32_t BX = (n + 1) >> 1, BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
+    const uint32_t GZ = (BZ + group - 1) / group;  // units along z
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
     // Unit (bx, by, gz), advanced by the grid stride in the same mixed radix.
     const uint32_t u0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t gz = u0 % W, by = (u0 / W) % BY, bx = u0 / (W * BY);
-    const uint32_t sz = nwarps % W, sy = (nwarps / W) % BY, sx = nwarps / (W * BY);
+    uint32_t gz = u0 % GZ, by = (u0 / GZ) % BY, bx = u0 / (GZ * BY);
+    const uint32_t sz = nwarps % GZ, sy = (nwarps / GZ) % BY, sx = nwarps / (GZ * BY);
     for (; bx < BX;) {
         const uint32_t x = 2 * bx + dx, y = 4 * by + dy;
         const bool row_ok = x < n && y < n;
         const float px = grid_coord(g, 0, x), py = grid_coord(g, 1, y);
-        const uint32_t bz_end = min(8 * gz + 8, BZ);
+        const uint32_t bz0 = gz * group, bz_end = min(bz0 + group, BZ);
         uint32_t word = 0;
-        for (uint32_t bz = 8 * gz; bz < bz_end; ++bz) {
+        for (uint32_t bz = bz0; bz < bz_end; ++bz) {
             const uint32_t z = 4 * bz + dz;
             bool pos = false;
             if (row_ok && z < n) {
@@ -99,11 +103,15 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
                 word |= ((b >> (lane & ~3u)) & 0xFu) << ((4 * bz) & 31);
             }
         }
-        if (sgn && dz == 0 && row_ok) sgn[(x * n + y) * W + gz] = word;
+        if (sgn && dz == 0 && row_ok) {
+            uint32_t* wp = &sgn[(x * n + y) * W + ((4 * bz0) >> 5)];
+            if (group == 8) *wp = word;
+            else if (word) atomicOr(wp, word);
+        }
         gz += sz;
         uint32_t carry = 0;
-        if (gz >= W) {
-            gz -= W;
+        if (gz >= GZ) {
+            gz -= GZ;
             carry = 1;
         }
         by += sy + carry;
@@ -310,10 +318,14 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
         const uint64_t b4 = (g.n + 3) >> 2;
         k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
     } else if (k != DE_GRID_LINEAR) {
-        // W words per row; without sign words the same (bx, by, gz) walk.
-        const uint32_t Wz = sgn ? W : (g.n + 31) / 32;
-        const uint64_t units = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2) * Wz;
-        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, Wz);
+        // 8-brick units when they make at least four waves of resident warps
+        // (8 blocks of 256 threads per SM), single bricks otherwise.
+        const uint64_t rows = (uint64_t)((g.n + 1) >> 1) * ((g.n + 3) >> 2);
+        const uint64_t bz = (g.n + 3) >> 2;
+        const uint64_t units8 = rows * ((bz + 7) / 8);
+        const uint32_t group = units8 >= 4ull * sm_count() * 8 * (B / 32) ? 8u : 1u;
+        const uint64_t units = rows * ((bz + group - 1) / group);
+        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, group);
     } else {
         const uint64_t total = (uint64_t)g.n * g.n * g.n;
         k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W);

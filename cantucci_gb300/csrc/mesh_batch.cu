@@ -46,7 +46,7 @@ struct BatchJob {
     uint32_t row_begin;         // first global cell row
     uint32_t item_begin;        // first global step-1 work item
     uint32_t items;
-    uint32_t brick;             // 1: 2x4x4 bricks, 0: 32 consecutive corners
+    uint32_t brick;             // 1: runs of 8 2x4x4 bricks along z, 0: 32 consecutive corners
 };
 
 struct BatchTotals {
@@ -55,7 +55,7 @@ struct BatchTotals {
 
 // Defaults of new batches (cg_set_option "batch_chunk", "batch_block",
 // "batch_brick_min_res", "batch_place_block").
-static cg_batch_tuning g_batch_default = {256, 64, 32, 128};
+static cg_batch_tuning g_batch_default = {256, 4, 8, 128};
 
 static bool valid_block(int64_t v, int64_t hi) {
     return v >= 64 && v <= hi && (v & (v - 1)) == 0;
@@ -116,20 +116,28 @@ __global__ void k_batch_de(ShapeDev s, const BatchJob* __restrict__ jobs, uint32
             uint32_t* sg = sgn + J.sgn_off;
             const uint32_t local = item - J.item_begin;
             if (J.brick) {
+                // Unit (bx, by, gz): the 8 bricks along z of sign word gz, as
+                // k_de_grid_brick walks them; the word is stored whole.
                 const uint32_t BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
-                const uint32_t bz = local % BZ, t = local / BZ, by = t % BY, bx = t / BY;
+                const uint32_t gz = local % W, t = local / W, by = t % BY, bx = t / BY;
                 const uint32_t dx = lane >> 4, dy = (lane >> 2) & 3, dz = lane & 3;
-                const uint32_t x = 2 * bx + dx, y = 4 * by + dy, z = 4 * bz + dz;
-                uint32_t bit = 0;
-                if (x < n && y < n && z < n) {
-                    const float d = eval<M>(s, job_coord(J, 0, x), job_coord(J, 1, y),
-                                            job_coord(J, 2, z));
-                    out[((size_t)x * n + y) * n + z] = d;
-                    bit = (__float_as_uint(d) >> 31) ? 0u : (1u << (z & 31));
+                const uint32_t x = 2 * bx + dx, y = 4 * by + dy;
+                const bool row_ok = x < n && y < n;
+                const float px = job_coord(J, 0, x), py = job_coord(J, 1, y);
+                const uint32_t bz_end = min(8 * gz + 8, BZ);
+                uint32_t word = 0;
+                for (uint32_t bz = 8 * gz; bz < bz_end; ++bz) {
+                    const uint32_t z = 4 * bz + dz;
+                    bool pos = false;
+                    if (row_ok && z < n) {
+                        const float d = eval<M>(s, px, py, job_coord(J, 2, z));
+                        out[((size_t)x * n + y) * n + z] = d;
+                        pos = (__float_as_uint(d) >> 31) == 0u;
+                    }
+                    const uint32_t b = __ballot_sync(0xFFFFFFFFu, pos);
+                    word |= ((b >> (lane & ~3u)) & 0xFu) << ((4 * bz) & 31);
                 }
-                bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 1);
-                bit |= __shfl_xor_sync(0xFFFFFFFFu, bit, 2);
-                if (dz == 0 && bit) atomicOr(&sg[(x * n + y) * W + (z >> 5)], bit);
+                if (dz == 0 && row_ok) sg[(x * n + y) * W + gz] = word;
             } else {
                 const uint32_t i = local * 32 + lane;
                 if (i < n * n * n) {
@@ -296,7 +304,7 @@ cg_status plan_items(std::vector<BatchJob>& jobs, uint32_t brick_min_res, uint32
     for (BatchJob& J : jobs) {
         const uint64_t n = J.d.n;
         J.brick = J.d.res >= brick_min_res ? 1u : 0u;
-        J.items = J.brick ? (uint32_t)(((n + 1) >> 1) * ((n + 3) >> 2) * ((n + 3) >> 2))
+        J.items = J.brick ? (uint32_t)(((n + 1) >> 1) * ((n + 3) >> 2) * J.d.W)
                           : (uint32_t)((n * n * n + 31) / 32);
         J.item_begin = (uint32_t)items;
         items += J.items;

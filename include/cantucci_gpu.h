@@ -292,8 +292,9 @@ cg_status cg_batch_set_jobs(cg_batch* batch, const cg_span_job* jobs, uint32_t n
  *                  on the GPU at once)
  *   de_chunk       step-1 work items a warp takes from the queue per grab
  *                  (1..4096)
- *   brick_min_res  spans with resolution >= this are walked in 2x4x4 corner
- *                  bricks per warp, smaller ones in runs of 32 corners
+ *   brick_min_res  spans with resolution >= this are walked in runs of eight
+ *                  2x4x4 corner bricks along z per work item (one sign word
+ *                  per row), smaller ones in runs of 32 corners
  *   place_block    threads per block of vertex placement (64, 128, 256) */
 typedef struct cg_batch_tuning {
     uint32_t de_block;
@@ -486,7 +487,7 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
  * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic.
  * All variants give bit-identical results.  "batch_block", "batch_chunk",
  * "batch_brick_min_res", "batch_place_block": the cg_batch_tuning that
- * batches created afterwards start with (defaults 256, 64, 32, 128). */
+ * batches created afterwards start with (defaults 256, 4, 8, 128). */
 cg_status cg_set_option(const char* name, int64_t value);
 
 /* The cudaStream_t (as void*) the mesher launches on, so a caller can time
