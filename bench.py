@@ -38,8 +38,8 @@ FLOPS_PER_STEP = 76   # P=8 iteration: magnitude, dr, polynomial, + p (each op =
 FLOPS_PER_ESCAPE = 6  # the final magnitude of an escaping point
 FLOPS_PER_POINT = 4   # ln(r) * r, * 0.5, / dr
 # DRAM bytes of one k_de_grid_brick launch on the 513^3-corner span, from ncu:
-# 83,462,144 read + 562,878,464 written (algorithmic: 557,918,280 written).
-DE_TRAFFIC_RES512 = 83_462_144 + 562_878_464
+# 63,769,856 read + 560,420,096 written (algorithmic: 557,918,280 written).
+DE_TRAFFIC_RES512 = 63_769_856 + 560_420_096
 LAUNCHES_PER_MESH = 12  # k_de_grid_brick (sign words fused), k_cells, 3x scan, k_vertex_list,
 #                         k_place, k_quad_count, 3x scan, k_quad_emit (ncu launch list: 12 per mesh)
 
@@ -859,8 +859,8 @@ def run_ours(args, rank, world, local_rank):
     elif res == RES and args.de_kernel in (0, 2):
         roofline["traffic"] = DE_TRAFFIC_RES512
         # pipe utilisation of the same launch in the same ncu capture
-        roofline["ncu_pipe_active"] = {"fma": 0.610, "alu": 0.259, "xu": 0.121,
-                                       "issue_slots": 0.891}
+        roofline["ncu_pipe_active"] = {"fma": 0.604, "alu": 0.226, "xu": 0.134,
+                                       "issue_slots": 0.882}
         roofline["traffic_source"] = ("dram__bytes_read.sum + dram__bytes_write.sum of one "
                                       "k_de_grid_brick launch at res 512 (ncu --set full, "
                                       "profiles/k_de_grid_brick_res512.md)")
