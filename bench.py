@@ -414,20 +414,21 @@ def extra_de_variants(dev, res=RES):
     return res_out
 
 
-def extra_polar_mesh_normals(dev, res=RES):
-    """The span mesher on the polar Mandelbulb (power 8.0, max_iters 15) at
-    513^3 corners with the reference's six-sample normals and with analytic
-    (forward-mode) normals: same vertices, DE values and indices; step 2
-    time compared."""
+def _mesh_normals(dev, shape, workload, res, oshape=None):
+    """The span mesher at res with the reference's six-sample normals and
+    with analytic (forward-mode) normals: same vertices, DE values and
+    indices; stage times, and with `oshape` (CPU legs only) the angle of
+    both normals to the FP64 gradient at 2000 sampled vertices."""
+    import numpy as np
     import torch
     import cantucci_gb300 as cg
     from cantucci_gb300 import workloads as W
     span = cg.Span(*W.SPAN_C1)
-    shape = cg.MandelbulbPolar(8.0, 15, 2.5)
     vcap, icap = res ** 3 // 16, 18 * res ** 3 // 16
     v = torch.empty((vcap, 7), dtype=torch.float32, device=dev)
     i = torch.empty(icap, dtype=torch.int32, device=dev)
-    out = {"workload": "polar Mandelbulb power 8.0, max_iters 15, %d^3 corners" % (res + 1)}
+    out = {"workload": workload}
+    verts = {}
     m = cg.Mesher(dev)
     try:
         for mode in ("fd", "analytic"):
@@ -442,11 +443,47 @@ def extra_polar_mesh_normals(dev, res=RES):
                          "step3_ms": min(t.third_ms for t in tms),
                          "mesh_ms": min(t.first_ms + t.second_ms + t.third_ms for t in tms),
                          "vertices": nv, "indices": ni}
+            verts[mode] = v[:nv].cpu().numpy()
     finally:
         m.close()
     out["step2_speedup"] = out["fd"]["step2_ms"] / out["analytic"]["step2_ms"]
     out["mesh_speedup"] = out["fd"]["mesh_ms"] / out["analytic"]["mesh_ms"]
+    out["same_positions_de"] = bool(np.array_equal(
+        verts["fd"][:, [0, 1, 2, 6]].view(np.uint32),
+        verts["analytic"][:, [0, 1, 2, 6]].view(np.uint32)))
+    if oshape is not None:
+        import oracle
+        rng = np.random.default_rng(5)
+        sel = rng.choice(len(verts["fd"]), size=min(2000, len(verts["fd"])), replace=False)
+        g = oracle.de_grad_f64(oshape, verts["fd"][sel, :3])[:, 1:4]
+        ok = np.all(np.isfinite(g), axis=1)
+        for mode in ("fd", "analytic"):
+            nrm = verts[mode][sel][ok, 3:6].astype(np.float64)
+            gg = g[ok] / np.linalg.norm(g[ok], axis=1, keepdims=True)
+            c = np.sum(nrm / np.linalg.norm(nrm, axis=1, keepdims=True) * gg, axis=1)
+            ang = np.degrees(np.arccos(np.clip(c, -1, 1)))
+            out[mode]["angle_deg_vs_fp64"] = {"median": float(np.median(ang)),
+                                              "frac_le_0.1": float(np.mean(ang <= 0.1))}
     return out
+
+
+def extra_polar_mesh_normals(dev, res=RES):
+    """Six-sample vs analytic normals on the polar Mandelbulb (power 8.0)."""
+    import cantucci_gb300 as cg
+    return _mesh_normals(dev, cg.MandelbulbPolar(8.0, 15, 2.5),
+                         "polar Mandelbulb power 8.0, max_iters 15, %d^3 corners" % (res + 1), res)
+
+
+def extra_p8_mesh_normals(dev, res=RES, cpu=True):
+    """Six-sample vs analytic normals on the reference's Mandelbulb<8> (the
+    polynomial differentiated in dual numbers)."""
+    import cantucci_gb300 as cg
+    oshape = None
+    if cpu:
+        import oracle
+        oshape = oracle.mandelbulb(**SHAPE)
+    return _mesh_normals(dev, cg.Mandelbulb(**SHAPE),
+                         "Mandelbulb P=8 max_iters 15, %d^3 corners" % (res + 1), res, oshape)
 
 
 def extra_fp64_check(dev, res=RES, stride=67):
@@ -705,6 +742,7 @@ def run_extras(args, dev):
             ("batched_spans", lambda: extra_batched(dev, cpu)),
             ("normals", lambda: extra_normals(dev, cpu=cpu)),
             ("polar_mesh_normals", lambda: extra_polar_mesh_normals(dev)),
+            ("p8_mesh_normals", lambda: extra_p8_mesh_normals(dev, cpu=cpu)),
             ("root_crossings", lambda: extra_root_crossings(dev)),
             ("dual_contouring", lambda: extra_dual_contouring(dev)),
             ("fast_numerics", lambda: extra_fast_numerics(dev)),

@@ -274,8 +274,8 @@ class Mesher:
 
     def set_normals(self, mode: str):
         """"fd": the reference's six-sample central difference (default);
-        "analytic": the forward-mode gradient, one pass per vertex (polar
-        Mandelbulb only)."""
+        "analytic": the forward-mode gradient, one pass per vertex (any
+        shape)."""
         modes = {"fd": _ffi.CG_NORMALS_FD, "analytic": _ffi.CG_NORMALS_ADJOINT}
         check(self._lib.cg_mesher_set_normals(self.handle, modes[mode]))
 

@@ -2,6 +2,7 @@
 // argument checks (the reference's assert! panics become CG_EINVAL), span
 // set-up in the reference's f32 operation order, the mesher object and its
 // device workspace.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -165,6 +166,12 @@ struct cg_mesher {
 
 namespace {
 
+// 1 (default): meshers created afterwards give their side stream (quads,
+// index copies) the highest stream priority, so its short kernels take
+// SMs ahead of the placement's waiting blocks (cg_set_option
+// "side_stream_priority"; 0: equal priorities).
+std::atomic<int> g_side_priority{1};
+
 PlaceOptions place_options(cg_mesher* m) {
     PlaceOptions o;
     o.analytic_normals = m->normals == CG_NORMALS_ADJOINT;
@@ -204,10 +211,6 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
                    cg_timings* tm) {
     CG_TRY(check_span_res(span, res));
     CG_TRY(check_shape(shape));
-    if (m->normals == CG_NORMALS_ADJOINT && shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
-        set_error("analytic normals are built for the polar Mandelbulb (kind 2) only");
-        return CG_EINVAL;
-    }
     const ShapeDev s = make_shape_dev(*shape);
     const SpanSetup su = setup_span(*span, res);
     const MeshDims d = mesh_dims(res);
@@ -260,10 +263,6 @@ cg_status run_mesh_to_host(cg_mesher* m, const cg_span* span, const cg_shape* sh
                            cg_timings* tm) {
     CG_TRY(check_span_res(span, res));
     CG_TRY(check_shape(shape));
-    if (m->normals == CG_NORMALS_ADJOINT && shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
-        set_error("analytic normals are built for the polar Mandelbulb (kind 2) only");
-        return CG_EINVAL;
-    }
     const ShapeDev s = make_shape_dev(*shape);
     const SpanSetup su = setup_span(*span, res);
     const MeshDims d = mesh_dims(res);
@@ -397,7 +396,10 @@ cg_status cg_mesher_create(int device, cg_mesher** out) {
     for (auto& e : m->ev) cudaEventCreate(&e);
     cudaEventCreateWithFlags(&m->fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&m->join, cudaEventDisableTiming);
-    if ((st = cuda_status(cudaStreamCreateWithFlags(&m->copy_stream, cudaStreamNonBlocking),
+    int prio_lo = 0, prio_hi = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess) prio_hi = prio_lo = 0;
+    if ((st = cuda_status(cudaStreamCreateWithPriority(&m->copy_stream, cudaStreamNonBlocking,
+                                                       g_side_priority.load() ? prio_hi : prio_lo),
                           "cudaStreamCreate", __FILE__, __LINE__)) != CG_OK) {
         cg_mesher_destroy(m);
         return st;
@@ -569,6 +571,11 @@ cg_status cg_set_option(const char* name, int64_t value) {
         return CG_OK;
     if (name && set_batch_option(name, value)) return CG_OK;
     if (name && set_trace_option(name, value)) return CG_OK;
+    if (name && set_place_option(name, value)) return CG_OK;
+    if (name && strcmp(name, "side_stream_priority") == 0 && (value == 0 || value == 1)) {
+        g_side_priority.store((int)value);
+        return CG_OK;
+    }
     set_error("unknown option or value: %s = %lld", name ? name : "(null)", (long long)value);
     return CG_EINVAL;
 }

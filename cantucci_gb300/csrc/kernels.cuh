@@ -51,6 +51,7 @@ cg_status launch_march(const ShapeDev& s, const float* org, const float* dir, ui
                        uint32_t max_steps, float eps, float* hits, uint8_t* hit, cudaStream_t st);
 // cg_set_option knobs of the depth-map march (trace.cu).
 int set_trace_option(const char* name, int64_t v);
+int set_place_option(const char* name, int64_t v);
 // Shape argument checks of the C ABI (kind, power, max_iters).
 cg_status check_shape(const cg_shape* s);
 
@@ -85,11 +86,6 @@ MeshDims mesh_dims(uint32_t res);
 // Byte size of a workspace for `res`; fills `w` with offsets from `base`.
 size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 
-// Vertex placement options of the span mesher; the defaults are the
-// reference's placement.  analytic_normals (polar form only) replaces the
-// six-sample normal by the forward-mode gradient; root_iters > 0 places edge
-// crossings at the DE's root along each edge; qef places the vertex at the
-// dual-contouring minimiser of the crossings' tangent planes.
 // A grow-only device buffer owned by the caller.
 struct DeviceScratch {
     void* ptr = nullptr;
@@ -97,6 +93,11 @@ struct DeviceScratch {
 };
 cg_status grow_scratch(DeviceScratch* b, size_t bytes);
 
+// Vertex placement options of the span mesher; the defaults are the
+// reference's placement.  analytic_normals replaces the
+// six-sample normal by the forward-mode gradient; root_iters > 0 places edge
+// crossings at the DE's root along each edge; qef places the vertex at the
+// dual-contouring minimiser of the crossings' tangent planes.
 // With qef the crossings go into an edge table first (one crossing and
 // gradient per sign-changing edge, shared by the edge's cells): its per-row
 // part lives in edge_rows, its per-edge part in edge_data; both are

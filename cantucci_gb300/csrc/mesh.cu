@@ -2,6 +2,9 @@
 // (MeshBuffer::naive_surface_nets, src/mesh/buffer.rs:85-372) on one span.
 // The per-row and per-vertex bodies (and the data layout) are in
 // mesh_rows.cuh; the batched multi-span version is mesh_batch.cu.
+#include <atomic>
+#include <cstring>
+
 #include "common.cuh"
 #include "kernels.cuh"
 #include "mesh_rows.cuh"
@@ -259,12 +262,26 @@ PlaceParams place_params(const SpanSetup& su) {
     return pp;
 }
 
+// Blocks of k_place per SM (cg_set_option "place_blocks_per_sm").  Many
+// short blocks (128 per SM, about 14 waves) rather than one resident wave:
+// blocks then finish throughout the launch, so the quad kernels on the
+// higher-priority side stream get SMs early and end under the placement
+// (measured on the 513^3 span: 3.39 ms per mesh against 3.45 with 16 per
+// SM and equal priorities).
+static std::atomic<uint32_t> g_place_blocks_per_sm{128};
+
+int set_place_option(const char* name, int64_t v) {
+    if (strcmp(name, "place_blocks_per_sm") || v < 1 || v > 1024) return 0;
+    g_place_blocks_per_sm.store((uint32_t)v);
+    return 1;
+}
+
 template <int M, bool AN>
 static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                               cudaStream_t st, const PlaceOptions& opt, const EdgeTable& et) {
     const unsigned B = 128;
-    const unsigned G = (unsigned)sm_count() * 16;
+    const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
     if (opt.qef)
         k_place<M, AN, false, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                      verts, vcap, 0, et);
@@ -371,7 +388,7 @@ static void launch_place_plain(const ShapeDev& s, const PlaceParams& pp, const M
                                const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                cudaStream_t st) {
     const unsigned B = 128;
-    const unsigned G = (unsigned)sm_count() * 16;
+    const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
     k_place<M, false, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                      verts, vcap, 0, EdgeTable{});
 }
@@ -390,23 +407,18 @@ static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const Mesh
     case MODE_P8_FAST: launch_place_plain<MODE_P8_FAST>(s, pp, d, w, verts, vcap, st); break;
     case MODE_INT_POLY: launch_place_plain<MODE_INT_POLY>(s, pp, d, w, verts, vcap, st); break;
     case MODE_POLAR_FAST: launch_place_plain<MODE_POLAR_FAST>(s, pp, d, w, verts, vcap, st); break;
-    case MODE_P8:
-        // (the rolled loop: with seven estimator calls per vertex the
-        // unrolled one measured slower here)
-        launch_place_mode<MODE_P8, false>(s, pp, d, w, verts, vcap, st, opt, et);
-        break;
-    case MODE_INT:
-        launch_place_mode<MODE_INT, false>(s, pp, d, w, verts, vcap, st, opt, et);
-        break;
-    case MODE_POLAR:
-        if (opt.analytic_normals)
-            launch_place_mode<MODE_POLAR, true>(s, pp, d, w, verts, vcap, st, opt, et);
-        else
-            launch_place_mode<MODE_POLAR, false>(s, pp, d, w, verts, vcap, st, opt, et);
-        break;
-    default:
-        launch_place_mode<MODE_SPHERE, false>(s, pp, d, w, verts, vcap, st, opt, et);
-        break;
+#define CG_PLACE_MODE(MODE)                                                        \
+    if (opt.analytic_normals)                                                      \
+        launch_place_mode<MODE, true>(s, pp, d, w, verts, vcap, st, opt, et);      \
+    else                                                                           \
+        launch_place_mode<MODE, false>(s, pp, d, w, verts, vcap, st, opt, et);
+    // (P = 8 takes the rolled loop: with seven estimator calls per vertex the
+    // unrolled one measured slower here)
+    case MODE_P8: CG_PLACE_MODE(MODE_P8) break;
+    case MODE_INT: CG_PLACE_MODE(MODE_INT) break;
+    case MODE_POLAR: CG_PLACE_MODE(MODE_POLAR) break;
+    default: CG_PLACE_MODE(MODE_SPHERE) break;
+#undef CG_PLACE_MODE
     }
     CG_CHECK_LAUNCH("k_place");
     return CG_OK;

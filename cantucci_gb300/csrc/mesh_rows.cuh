@@ -204,9 +204,10 @@ __device__ __forceinline__ float linear_root(float f0, float f1) {
 
 // Vertex of one surface cell (buffer.rs:149-274): centroid of the lerped edge
 // crossings, DE at the vertex and the six-sample central-difference normal.
-// With AN (polar form only) the normal is instead the normalised analytic
-// gradient from one forward-mode pass, which also gives the DE at the vertex
-// (the same bits as the estimator's).  With ROOT each crossing is not the
+// With AN the normal is instead the normalised analytic gradient from one
+// forward-mode pass (shape_gradient: for P = 8 the reference's polynomial
+// in dual numbers), which also gives the DE at the vertex (the same bits as
+// the estimator's; for other integer powers one more estimator call).  With ROOT each crossing is not the
 // reference's distance-weighted lerp but the root of the DE along the edge,
 // found by root_iters Illinois (regula falsi) steps from the edge's corner
 // distances -- the refinement buffer.rs:178-186 leaves for
@@ -314,8 +315,9 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
     // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
     // loop is kept rolled so that one copy of the estimator is in the code.
     if constexpr (AN) {
-        float g[5];
-        polar_de_tangent<3, false>(s, nullptr, vx, vy, vz, g);
+        float g[4];
+        shape_gradient<M>(s, vx, vy, vz, g);
+        if constexpr (M == MODE_INT) g[0] = eval<M>(s, vx, vy, vz);  // the estimator's bits
         const float inv = __fdiv_rn(1.0f, magnitude<Exact>(g[1], g[2], g[3]));
         if (o) {
             o[0] = vx;

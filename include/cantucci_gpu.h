@@ -59,7 +59,7 @@ enum {
 enum {
     CG_NORMALS_FD = 0,      /* six central differences, as buffer.rs:256-266 */
     CG_NORMALS_ADJOINT = 1  /* analytic dDE/dp, one forward-mode pass per vertex instead of
-                               six extra estimator calls; polar Mandelbulb only (new) */
+                               six extra estimator calls; any shape (new) */
 };
 
 /* Edge crossings of the mesher. */
@@ -155,10 +155,12 @@ typedef struct cg_mesher cg_mesher;
 /* A mesher owns a stream, events and a grow-only device workspace. */
 cg_status cg_mesher_create(int device, cg_mesher** out);
 void cg_mesher_destroy(cg_mesher* mesher);
-/* Select the normals (CG_NORMALS_FD default).  With CG_NORMALS_ADJOINT a
- * mesh of any shape but the polar Mandelbulb fails with CG_EINVAL; vertex
- * positions, DE values and indices are unchanged, only the normals differ
- * from the reference's six-sample difference. */
+/* Select the normals (CG_NORMALS_FD default).  With CG_NORMALS_ADJOINT each
+ * vertex's normal is the normalised gradient of the DE there, one
+ * forward-mode pass (for Mandelbulb<8> the reference's polynomial,
+ * mandelbulb.rs:148-200, in dual numbers); vertex positions, DE values and
+ * indices are unchanged, only the normals differ from the reference's
+ * six-sample difference. */
 cg_status cg_mesher_set_normals(cg_mesher* mesher, uint32_t normals);
 /* Select the edge crossings (CG_CROSSINGS_LERP default).  CG_CROSSINGS_ROOT
  * refines each crossing with `iters` (1..16) Illinois steps on the DE along
@@ -483,9 +485,13 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
 /* ---- measurement -------------------------------------------------------- */
 
 /* Process-wide tuning knobs.  "de_grid_kernel": 0 auto, 1 one corner per
- * thread in GridTable order, 2 one 2x4x4 brick per warp, 3 (P=8 only) one
+ * thread in GridTable order, 2 2x4x4 bricks per warp, 3 (P=8 only) one
  * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic.
- * All variants give bit-identical results.  "batch_block", "batch_chunk",
+ * "place_blocks_per_sm" (1..1024, default 128): the vertex placement's grid.
+ * "side_stream_priority" (1 default, or 0): whether meshers created
+ * afterwards run their quads and copies on a highest-priority stream.
+ * "trace_kernel": 1 work-queue march (default), 0 one pixel per thread.
+ * None of these changes an output bit.  "batch_block", "batch_chunk",
  * "batch_brick_min_res", "batch_place_block": the cg_batch_tuning that
  * batches created afterwards start with (defaults 256, 4, 8, 128). */
 cg_status cg_set_option(const char* name, int64_t value);

@@ -176,7 +176,7 @@ public:
     Mesher& operator=(const Mesher&) = delete;
     cg_mesher* get() const { return m_; }
 
-    // CG_NORMALS_FD (the reference's) or CG_NORMALS_ADJOINT (polar form).
+    // CG_NORMALS_FD (the reference's) or CG_NORMALS_ADJOINT (analytic, any shape).
     void set_normals(uint32_t normals) { check(cg_mesher_set_normals(m_, normals)); }
     // CG_CROSSINGS_LERP (the reference's) or CG_CROSSINGS_ROOT with 1..16 steps.
     void set_crossings(uint32_t crossings, uint32_t iters = 4) {
