@@ -419,3 +419,29 @@ def test_fast_numerics_mesh(cg, kind):
     lo = (start + cells.astype(np.float32) * step).astype(np.float32)
     ok = np.all((b[order, :3] >= lo - 1e-6) & (b[order, :3] <= lo + step + 1e-6), axis=1)
     assert ok.all()
+
+
+def test_launch_knobs_change_no_bit(cg):
+    """The placement grid and the side stream's priority are launch shapes
+    only: meshes under other settings equal the default mesh bit for bit."""
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    lib = cg.load()
+    meshes = []
+    try:
+        for bps, prio in ((128, 1), (1, 0), (16, 1), (1024, 0)):
+            assert lib.cg_set_option(b"place_blocks_per_sm", bps) == 0
+            assert lib.cg_set_option(b"side_stream_priority", prio) == 0
+            m = cg.Mesher(0)
+            try:
+                v, i, nv, ni, _ = m.generate(span, s, 128)
+            finally:
+                m.close()
+            meshes.append((as7(v[:nv]).view(np.uint32).copy(), i[:ni].copy()))
+        assert lib.cg_set_option(b"place_blocks_per_sm", 0) != 0
+        assert lib.cg_set_option(b"side_stream_priority", 2) != 0
+    finally:
+        lib.cg_set_option(b"place_blocks_per_sm", 128)
+        lib.cg_set_option(b"side_stream_priority", 1)
+    for v, i in meshes[1:]:
+        assert np.array_equal(v, meshes[0][0]) and np.array_equal(i, meshes[0][1])
