@@ -731,6 +731,44 @@ def extra_fast_numerics(dev, res=RES):
     return out
 
 
+def extra_leaf_pool(dev, threads=(1, 2, 4, 8)):
+    """The reference's call pattern for the same 512 depth-3 leaves the CPU
+    baseline meshes (res 64 each): T host threads, each with its own mesher,
+    each call the blocking generate_for_box into pageable numpy arrays, as
+    ShapeMesh's thread pool calls it (src/mesh/mod.rs:141-148).  Whole-job
+    leaves/s and corners/s per T."""
+    import numpy as np
+    import cantucci_gb300 as cg
+    leaves = leaf_spans(3)
+    shape = cg.Mandelbulb(**SHAPE)
+    out = {"workload": "512 depth-3 leaves of [-1.2,1.2]^3 at res 64 (140,608,000 corners), "
+                       "Mandelbulb P=8 max_iters 15, pageable host outputs"}
+    for T in threads:
+        meshers = [cg.Mesher(dev) for _ in range(T)]
+        bufs = [(np.empty(64 ** 3, cg.VERTEX_DTYPE), np.empty(18 * 64 ** 3, np.uint32))
+                for _ in range(T)]
+
+        def work(k):
+            m, (vb, ib) = meshers[k], bufs[k]
+            nv = 0
+            for j in range(k, len(leaves), T):
+                _, _, a, _, _ = m.generate(leaves[j], shape, 64, vertices=vb, indices=ib)
+                nv += a
+            return nv
+
+        for k in range(T):  # warm-up: one leaf per mesher
+            meshers[k].generate(leaves[k], shape, 64, vertices=bufs[k][0], indices=bufs[k][1])
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=T) as ex:
+            nv = sum(ex.map(work, range(T)))
+        dt = time.perf_counter() - t0
+        for m in meshers:
+            m.close()
+        out["threads_%d" % T] = {"seconds": dt, "leaves_per_s": len(leaves) / dt,
+                                 "corners_per_s": len(leaves) * 65 ** 3 / dt, "vertices": int(nv)}
+    return out
+
+
 def run_extras(args, dev):
     """The other configurations.  The oracle runs only in CPU legs (the CPU
     builder's timing and the accuracy checks against FP64), which
@@ -747,6 +785,7 @@ def run_extras(args, dev):
             ("dual_contouring", lambda: extra_dual_contouring(dev)),
             ("fast_numerics", lambda: extra_fast_numerics(dev)),
             ("lod", lambda: extra_lod(dev, cpu)),
+            ("leaf_pool", lambda: extra_leaf_pool(dev)),
             ("depth_fit", lambda: extra_depth_fit(dev, args.fit_steps))]
     if cpu:
         legs.insert(1, ("fp64_check", lambda: extra_fp64_check(dev)))
