@@ -78,8 +78,9 @@ __global__ void __launch_bounds__(128) k_de_spatial_grad(ShapeDev s, const float
 }
 
 // Vector-Jacobian product of a batch: g[i] * dDE/dp into grad_points (n x 3)
-// and the sum over points of g[i] * dDE/d(power, euler) into params (4
-// floats, accumulated with atomics; zero it first).
+// and, per warp, the sum over its points of g[i] * dDE/d(power, euler) into
+// partial[4 w .. 4 w + 3] (added up by k_sum_partials4 in a fixed order, so
+// the result does not depend on scheduling).
 __global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
                                                 const float* __restrict__ g, uint64_t n,
                                                 float* __restrict__ gp, float* __restrict__ params) {
@@ -103,13 +104,42 @@ __global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float*
         }
     }
     if (params) {
+        const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             float v = acc[k];
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-            if ((threadIdx.x & 31) == 0 && v != 0.0f) atomicAdd(&params[k], v);
+            if ((threadIdx.x & 31) == 0) params[4 * w + k] = v;
         }
     }
+}
+
+// params[k] += the sum over warps w < nwarps of partial[4 w + k], in a fixed
+// order (one block: strided sequential sums, then a fixed tree).
+__global__ void __launch_bounds__(256) k_sum_partials4(const float* __restrict__ partial,
+                                                       uint32_t nwarps, float* __restrict__ params) {
+    __shared__ float sh[4][256];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float v = 0.0f;
+        for (uint32_t w = threadIdx.x; w < nwarps; w += 256) v += partial[4 * w + k];
+        sh[k][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (uint32_t half = 128; half > 0; half >>= 1) {
+        if (threadIdx.x < half)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + half];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) params[threadIdx.x] += sh[threadIdx.x][0];
+}
+
+cg_status launch_sum_partials4(const float* partial, uint32_t nwarps, float* params,
+                               cudaStream_t st) {
+    k_sum_partials4<<<1, 256, 0, st>>>(partial, nwarps, params);
+    CG_CHECK_LAUNCH("k_sum_partials4");
+    return CG_OK;
 }
 
 // Central-difference gradient with six estimator evaluations per point
@@ -250,11 +280,16 @@ cg_status cg_de_backward(const cg_shape* shape, const float* points, const float
     cudaStream_t st = (cudaStream_t)stream;
     if (grad_params) CG_CUDA(cudaMemsetAsync(grad_params, 0, 4 * sizeof(float), st));
     if (!n) return CG_OK;
-    k_de_vjp<<<grid_for(n, 128, 16), 128, 0, st>>>(make_shape_dev(*shape),
-                                                    rotation_derivatives(*shape), points,
-                                                    grad_out, n, grad_points, grad_params);
-    CG_CHECK_LAUNCH("k_de_vjp");
-    return CG_OK;
+    const unsigned G = grid_for(n, 128, 16);
+    const uint32_t nwarps = G * 4;
+    float* partial = nullptr;
+    if (grad_params) CG_CUDA(cudaMallocAsync(&partial, (size_t)nwarps * 4 * sizeof(float), st));
+    k_de_vjp<<<G, 128, 0, st>>>(make_shape_dev(*shape), rotation_derivatives(*shape), points,
+                                grad_out, n, grad_points, partial);
+    cg_status rs = cuda_status(cudaGetLastError(), "k_de_vjp", __FILE__, __LINE__);
+    if (rs == CG_OK && partial) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
+    if (partial) cudaFreeAsync(partial, st);
+    return rs;
 }
 
 cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, float h, float* out,

@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "mesh_rows.cuh"
 
 namespace cg {
 
@@ -141,6 +142,23 @@ static cg_status check_span_res(const cg_span* span, uint32_t res) {
 
 using namespace cg;
 
+// The span-dependent parameters of a mesh, read from device memory by a
+// replayed graph.
+struct MeshGraphParams {
+    GridDev g;
+    PlaceParams pp;
+};
+
+// What a captured mesh graph depends on besides the span (compared bytewise).
+struct MeshGraphKey {
+    cg_shape shape;
+    uint32_t res, numerics, normals, root_iters, grid_kernel, place_bps;
+    const void* work;
+    const void* dverts;
+    const void* didx;
+    uint64_t vcap, icap;
+};
+
 struct cg_mesher {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -159,12 +177,24 @@ struct cg_mesher {
     uint32_t placement = CG_PLACEMENT_CENTROID;
     uint32_t numerics = CG_NUMERICS_EXACT;
     DeviceScratch edge_rows, edge_data;  // dual contouring's edge table
+    // The device-side mesh captured as a graph (run_mesh): replayed while the
+    // key matches, the span going in through the parameter block.
+    cudaGraphExec_t gexec = nullptr;
+    MeshGraphKey gkey{};
+    MeshGraphParams* gparams_dev = nullptr;
+    MeshGraphParams* gparams_host = nullptr;  // pinned
+    bool graph_broken = false;                // a capture failed: launch directly
     uint32_t last_res = 0;
     MeshWork last_w{};
     std::mutex mu;
 };
 
 namespace {
+
+// 1 (default): meshes up to resolution 128 without dual contouring replay a
+// graph captured per mesher (cg_set_option "mesh_graphs"; 0: direct
+// launches).
+std::atomic<int> g_mesh_graphs{1};
 
 // 1 (default): meshers created afterwards give their side stream (quads,
 // index copies) the highest stream priority, so its short kernels take
@@ -205,6 +235,97 @@ struct DeviceGuard {
     }
 };
 
+// Steps 1-3 into device outputs on m->stream, up to the counters' copy into
+// m->hcnt: what a mesh graph replays.  With `dp` the span's grid and
+// placement parameters are read from the device block dp (copied there from
+// the pinned m->gparams_host first).
+cg_status enqueue_mesh(cg_mesher* m, const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
+                       const MeshWork& w, cg_vertex* dverts, uint64_t vcap, uint32_t* didx,
+                       uint64_t icap, MeshGraphParams* dp) {
+    cudaStream_t st = m->stream;
+    if (dp)
+        CG_CUDA(cudaMemcpyAsync(dp, m->gparams_host, sizeof(MeshGraphParams),
+                                cudaMemcpyHostToDevice, st));
+    CG_CUDA(record_event(m->ev[0], st));
+    CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
+    CG_TRY(launch_de_grid(s, make_grid(su, d.res), w.dists, m->numerics, st, w.sgn, d.W,
+                          dp ? &dp->g : nullptr));
+    CG_CUDA(record_event(m->ev[1], st));
+    const SideStream side = {m->copy_stream, m->fork, m->join};
+    PlaceOptions opt = place_options(m);
+    opt.pp_dev = dp ? &dp->pp : nullptr;
+    CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
+                                  /*signs_ready=*/true, opt, &side));
+    CG_CUDA(record_event(m->ev[3], st));
+    CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
+    return CG_OK;
+}
+
+// Meshes into the graph kept for this mesher, capturing it first if the key
+// changed.  Only up to kGraphMaxRes: there the 12 launches cost about as
+// much as the work, while in a large mesh they are negligible and a
+// replayed graph loses the side stream's priority (its quads then end 0.2 ms
+// after the placement on the 513^3 span instead of under it).  Returns false
+// (nothing enqueued) if the mesh is not replayed: larger, dual contouring
+// (it reads the edge count back mid-way), or capturing failed.
+constexpr uint32_t kGraphMaxRes = 128;
+
+bool launch_mesh_graph(cg_mesher* m, const cg_shape* shape, const ShapeDev& s,
+                       const SpanSetup& su, const MeshDims& d, const MeshWork& w,
+                       cg_vertex* dverts, uint64_t vcap, uint32_t* didx, uint64_t icap) {
+    if (!g_mesh_graphs.load() || m->graph_broken || m->placement == CG_PLACEMENT_QEF ||
+        d.res > kGraphMaxRes)
+        return false;
+    if (!m->gparams_dev) {
+        if (cudaMalloc(&m->gparams_dev, sizeof(MeshGraphParams)) != cudaSuccess ||
+            cudaMallocHost(&m->gparams_host, sizeof(MeshGraphParams)) != cudaSuccess) {
+            cudaGetLastError();
+            m->graph_broken = true;
+            return false;
+        }
+    }
+    m->gparams_host->g = make_grid(su, d.res);
+    m->gparams_host->pp = place_params(su);
+    MeshGraphKey k;
+    memset(&k, 0, sizeof k);
+    k.shape = *shape;
+    k.res = d.res;
+    k.numerics = m->numerics;
+    k.normals = m->normals;
+    k.root_iters = m->root_iters;
+    k.grid_kernel = (uint32_t)de_grid_kernel_option();
+    k.place_bps = place_blocks_per_sm();
+    k.work = m->work;
+    k.dverts = dverts;
+    k.didx = didx;
+    k.vcap = vcap;
+    k.icap = icap;
+    if (!m->gexec || memcmp(&k, &m->gkey, sizeof k) != 0) {
+        if (m->gexec) cudaGraphExecDestroy(m->gexec);
+        m->gexec = nullptr;
+        cudaStream_t st = m->stream;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            m->graph_broken = true;
+            return false;
+        }
+        const cg_status cs = enqueue_mesh(m, s, su, d, w, dverts, vcap, didx, icap, m->gparams_dev);
+        cudaGraph_t gr = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(st, &gr);
+        cudaError_t ie = cudaErrorUnknown;
+        if (cs == CG_OK && ee == cudaSuccess && gr) ie = cudaGraphInstantiate(&m->gexec, gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+        if (ie != cudaSuccess) {
+            cudaGetLastError();
+            m->gexec = nullptr;
+            m->graph_broken = true;
+            return false;
+        }
+        m->gkey = k;
+    }
+    return cudaGraphLaunch(m->gexec, m->stream) == cudaSuccess;
+}
+
 // Runs steps 1-3 into device outputs; counts and status land in m->hcnt.
 cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uint32_t res,
                    cg_vertex* dverts, uint64_t vcap, uint32_t* didx, uint64_t icap,
@@ -218,17 +339,9 @@ cg_status run_mesh(cg_mesher* m, const cg_span* span, const cg_shape* shape, uin
     CG_TRY(ensure(reinterpret_cast<void**>(&m->work), &m->work_bytes, need));
     MeshWork w;
     mesh_workspace_layout(res, m->work, &w);
-    cudaStream_t st = m->stream;
-    CG_CUDA(cudaEventRecord(m->ev[0], st));
-    CG_CUDA(cudaMemsetAsync(w.sgn, 0, (size_t)d.n * d.n * d.W * sizeof(uint32_t), st));
-    CG_TRY(launch_de_grid(s, make_grid(su, res), w.dists, m->numerics, st, w.sgn, d.W));
-    CG_CUDA(cudaEventRecord(m->ev[1], st));
-    const SideStream side = {m->copy_stream, m->fork, m->join};
-    CG_TRY(launch_mesh_from_dists(s, su, d, w, dverts, vcap, didx, icap, st, m->ev[2],
-                                  /*signs_ready=*/true, place_options(m), &side));
-    CG_CUDA(cudaEventRecord(m->ev[3], st));
-    CG_CUDA(cudaMemcpyAsync(m->hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
-    CG_CUDA(cudaStreamSynchronize(st));
+    if (!launch_mesh_graph(m, shape, s, su, d, w, dverts, vcap, didx, icap))
+        CG_TRY(enqueue_mesh(m, s, su, d, w, dverts, vcap, didx, icap, nullptr));
+    CG_CUDA(cudaStreamSynchronize(m->stream));
     m->last_res = res;
     m->last_w = w;
     if (tm) {
@@ -421,6 +534,9 @@ void cg_mesher_destroy(cg_mesher* m) {
     if (m->dverts) cudaFree(m->dverts);
     if (m->didx) cudaFree(m->didx);
     if (m->hcnt) cudaFreeHost(m->hcnt);
+    if (m->gexec) cudaGraphExecDestroy(m->gexec);
+    if (m->gparams_dev) cudaFree(m->gparams_dev);
+    if (m->gparams_host) cudaFreeHost(m->gparams_host);
     if (m->edge_rows.ptr) cudaFree(m->edge_rows.ptr);
     if (m->edge_data.ptr) cudaFree(m->edge_data.ptr);
     for (auto& e : m->ev)
@@ -572,6 +688,10 @@ cg_status cg_set_option(const char* name, int64_t value) {
     if (name && set_batch_option(name, value)) return CG_OK;
     if (name && set_trace_option(name, value)) return CG_OK;
     if (name && set_place_option(name, value)) return CG_OK;
+    if (name && strcmp(name, "mesh_graphs") == 0 && (value == 0 || value == 1)) {
+        g_mesh_graphs.store((int)value);
+        return CG_OK;
+    }
     if (name && strcmp(name, "side_stream_priority") == 0 && (value == 0 || value == 1)) {
         g_side_priority.store((int)value);
         return CG_OK;

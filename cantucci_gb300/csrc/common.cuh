@@ -38,6 +38,15 @@ inline cg_status cuda_status(cudaError_t e, const char* what, const char* file, 
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// A timing event: while `st` is being captured into a graph, recorded as an
+// event node of the graph (so it times the replay), else recorded now.
+inline cudaError_t record_event(cudaEvent_t ev, cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        return cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+    return cudaEventRecord(ev, st);
+}
+
 // Grid size for a grid-stride kernel: enough blocks to fill every SM
 // `per_sm` times, never more than the work needs.
 inline unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm) {

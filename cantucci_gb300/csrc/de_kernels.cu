@@ -43,7 +43,9 @@ __device__ __forceinline__ float grid_coord(const GridDev& g, int k, uint32_t v)
 // `sgn`, also sets bit z%32 of sign word (x, y, z/32) for positive corners.
 template <int M>
 __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* __restrict__ out,
-                                                 uint32_t* __restrict__ sgn, uint32_t W) {
+                                                 uint32_t* __restrict__ sgn, uint32_t W,
+                                                 const GridDev* __restrict__ gp) {
+    if (gp) g = *gp;
     const uint32_t total = g.n * g.n * g.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
@@ -73,7 +75,9 @@ template <int M>
 __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
                                                        float* __restrict__ out,
                                                        uint32_t* __restrict__ sgn, uint32_t W,
-                                                       uint32_t group) {
+                                                       uint32_t group,
+                                                       const GridDev* __restrict__ gp) {
+    if (gp) g = *gp;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t n = g.n;
     const uint32_t BX = (n + 1) >> 1, BY = (n + 3) >> 2, BZ = (n + 3) >> 2;
@@ -259,7 +263,9 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
 // be zeroed first).
 __global__ void __launch_bounds__(256) k_de_grid_p8x2(ShapeDev s, GridDev g,
                                                       float* __restrict__ out,
-                                                      uint32_t* __restrict__ sgn, uint32_t W) {
+                                                      uint32_t* __restrict__ sgn, uint32_t W,
+                                                      const GridDev* __restrict__ gp) {
+    if (gp) g = *gp;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t n = g.n;
     const uint32_t B4 = (n + 3) >> 2;
@@ -302,6 +308,8 @@ __global__ void __launch_bounds__(256) k_de_grid_p8x2(ShapeDev s, GridDev g,
 // Kernel choice for step 1 (cg_set_option "de_grid_kernel").
 static int g_de_grid_kernel = DE_GRID_AUTO;
 
+int de_grid_kernel_option() { return g_de_grid_kernel; }
+
 int set_de_grid_kernel(int v) {
     if (v < DE_GRID_AUTO || v > DE_GRID_PACKED) return 0;
     g_de_grid_kernel = v;
@@ -310,13 +318,13 @@ int set_de_grid_kernel(int v) {
 
 template <int M>
 static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, uint32_t* sgn,
-                             uint32_t W, cudaStream_t st) {
+                             uint32_t W, cudaStream_t st, const GridDev* gp) {
     const unsigned B = 256;
     int k = g_de_grid_kernel;
     if (k == DE_GRID_AUTO) k = g.n >= 33 ? DE_GRID_BRICK : DE_GRID_LINEAR;
     if (k == DE_GRID_PACKED && (M == MODE_P8 || M == MODE_P8_IT15)) {
         const uint64_t b4 = (g.n + 3) >> 2;
-        k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+        k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, gp);
     } else if (k != DE_GRID_LINEAR) {
         // 8-brick units when they make at least four waves of resident warps
         // (8 blocks of 256 threads per SM), single bricks otherwise.
@@ -325,28 +333,28 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
         const uint64_t units8 = rows * ((bz + 7) / 8);
         const uint32_t group = units8 >= 4ull * sm_count() * 8 * (B / 32) ? 8u : 1u;
         const uint64_t units = rows * ((bz + group - 1) / group);
-        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, group);
+        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, group, gp);
     } else {
         const uint64_t total = (uint64_t)g.n * g.n * g.n;
-        k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W);
+        k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W, gp);
     }
 }
 
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
-                         cudaStream_t st, uint32_t* sgn, uint32_t W) {
+                         cudaStream_t st, uint32_t* sgn, uint32_t W, const GridDev* gp) {
     switch (mode_of(s, numerics)) {
     case MODE_P8:
-        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_IT15>(s, g, out, sgn, W, st);
-        else launch_grid_mode<MODE_P8>(s, g, out, sgn, W, st);
+        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_IT15>(s, g, out, sgn, W, st, gp);
+        else launch_grid_mode<MODE_P8>(s, g, out, sgn, W, st, gp);
         break;
-    case MODE_INT: launch_grid_mode<MODE_INT>(s, g, out, sgn, W, st); break;
-    case MODE_POLAR: launch_grid_mode<MODE_POLAR>(s, g, out, sgn, W, st); break;
-    case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st); break;
-    case MODE_INT_POLY: launch_grid_mode<MODE_INT_POLY>(s, g, out, sgn, W, st); break;
-    case MODE_POLAR_FAST: launch_grid_mode<MODE_POLAR_FAST>(s, g, out, sgn, W, st); break;
+    case MODE_INT: launch_grid_mode<MODE_INT>(s, g, out, sgn, W, st, gp); break;
+    case MODE_POLAR: launch_grid_mode<MODE_POLAR>(s, g, out, sgn, W, st, gp); break;
+    case MODE_SPHERE: launch_grid_mode<MODE_SPHERE>(s, g, out, sgn, W, st, gp); break;
+    case MODE_INT_POLY: launch_grid_mode<MODE_INT_POLY>(s, g, out, sgn, W, st, gp); break;
+    case MODE_POLAR_FAST: launch_grid_mode<MODE_POLAR_FAST>(s, g, out, sgn, W, st, gp); break;
     default:
-        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_FAST_IT15>(s, g, out, sgn, W, st);
-        else launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st);
+        if (p8_unrolled(s)) launch_grid_mode<MODE_P8_FAST_IT15>(s, g, out, sgn, W, st, gp);
+        else launch_grid_mode<MODE_P8_FAST>(s, g, out, sgn, W, st, gp);
         break;
     }
     CG_CHECK_LAUNCH("k_de_grid");

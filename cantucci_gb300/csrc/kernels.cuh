@@ -36,11 +36,17 @@ int set_batch_option(const char* name, int64_t v);
 // Step-1 kernel variants (cg_set_option "de_grid_kernel").
 enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3 };
 int set_de_grid_kernel(int v);
+int de_grid_kernel_option();
+uint32_t place_blocks_per_sm();
 
 // Step 1 on a span grid.  With `sgn` (zeroed, (res+1)^2 rows x W words) the
 // kernel also packs is_sign_positive of every corner into sign words.
+// With `gp` the kernels take the grid from device memory instead of `g`
+// (which still fixes the launch shape): a captured graph then serves every
+// span of the same resolution.
 cg_status launch_de_grid(const ShapeDev& s, const GridDev& g, float* out, uint32_t numerics,
-                         cudaStream_t st, uint32_t* sgn = nullptr, uint32_t W = 0);
+                         cudaStream_t st, uint32_t* sgn = nullptr, uint32_t W = 0,
+                         const GridDev* gp = nullptr);
 cg_status launch_grid_work(const ShapeDev& s, const GridDev& g, unsigned long long* acc,
                            cudaStream_t st);
 cg_status launch_state(const ShapeDev& s, const float* pts, uint64_t n, float* out,
@@ -86,6 +92,8 @@ MeshDims mesh_dims(uint32_t res);
 // Byte size of a workspace for `res`; fills `w` with offsets from `base`.
 size_t mesh_workspace_layout(uint32_t res, char* base, MeshWork* w);
 
+struct PlaceParams;  // mesh_rows.cuh
+
 // A grow-only device buffer owned by the caller.
 struct DeviceScratch {
     void* ptr = nullptr;
@@ -107,6 +115,7 @@ struct PlaceOptions {
     uint32_t root_iters = 0;
     bool qef = false;
     uint32_t numerics = CG_NUMERICS_EXACT;  // FAST: with none of the options above
+    const PlaceParams* pp_dev = nullptr;    // placement parameters in device memory (graphs)
     DeviceScratch* edge_rows = nullptr;
     DeviceScratch* edge_data = nullptr;
 };
@@ -148,5 +157,9 @@ cg_status launch_points_table(const MeshDims& d, const MeshWork& w, uint32_t* po
 cg_status launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
                                 uint32_t* total, cudaStream_t st);
 size_t scan_scratch_words(uint32_t n);
+// params[k] += the sum over nwarps per-warp partials partial[4 w + k], in a
+// fixed order (deterministic parameter gradients).
+cg_status launch_sum_partials4(const float* partial, uint32_t nwarps, float* params,
+                               cudaStream_t st);
 
 }  // namespace cg

@@ -98,7 +98,9 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
                                                const uint32_t* __restrict__ cellidx,
                                                MeshCounters* __restrict__ cnt,
                                                cg_vertex* __restrict__ verts, uint64_t vcap,
-                                               uint32_t root_iters, EdgeTable et) {
+                                               uint32_t root_iters, EdgeTable et,
+                                               const PlaceParams* __restrict__ ppp) {
+    if (ppp) pp = *ppp;
     __shared__ __align__(16) float stage[4][32 * 7];
     const uint32_t V = cnt->vertices;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -270,6 +272,8 @@ PlaceParams place_params(const SpanSetup& su) {
 // SM and equal priorities).
 static std::atomic<uint32_t> g_place_blocks_per_sm{128};
 
+uint32_t place_blocks_per_sm() { return g_place_blocks_per_sm.load(); }
+
 int set_place_option(const char* name, int64_t v) {
     if (strcmp(name, "place_blocks_per_sm") || v < 1 || v > 1024) return 0;
     g_place_blocks_per_sm.store((uint32_t)v);
@@ -284,13 +288,13 @@ static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const Me
     const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
     if (opt.qef)
         k_place<M, AN, false, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                     verts, vcap, 0, et);
+                                                     verts, vcap, 0, et, opt.pp_dev);
     else if (opt.root_iters)
         k_place<M, AN, true, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                     verts, vcap, opt.root_iters, et);
+                                                     verts, vcap, opt.root_iters, et, opt.pp_dev);
     else
         k_place<M, AN, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                      verts, vcap, 0, et);
+                                                      verts, vcap, 0, et, opt.pp_dev);
 }
 
 // The per-row part of the edge table for `res`: ecount, eoff (3 n^2 each),
@@ -386,11 +390,11 @@ static cg_status launch_edge_data(const ShapeDev& s, const PlaceParams& pp, cons
 template <int M>
 static void launch_place_plain(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
                                const MeshWork& w, cg_vertex* verts, uint64_t vcap,
-                               cudaStream_t st) {
+                               cudaStream_t st, const PlaceParams* pp_dev) {
     const unsigned B = 128;
     const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
     k_place<M, false, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
-                                                     verts, vcap, 0, EdgeTable{});
+                                                     verts, vcap, 0, EdgeTable{}, pp_dev);
 }
 
 static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
@@ -404,9 +408,9 @@ static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const Mesh
         return CG_EINVAL;
     }
     switch (mode_of(s, opt.numerics)) {
-    case MODE_P8_FAST: launch_place_plain<MODE_P8_FAST>(s, pp, d, w, verts, vcap, st); break;
-    case MODE_INT_POLY: launch_place_plain<MODE_INT_POLY>(s, pp, d, w, verts, vcap, st); break;
-    case MODE_POLAR_FAST: launch_place_plain<MODE_POLAR_FAST>(s, pp, d, w, verts, vcap, st); break;
+    case MODE_P8_FAST: launch_place_plain<MODE_P8_FAST>(s, pp, d, w, verts, vcap, st, opt.pp_dev); break;
+    case MODE_INT_POLY: launch_place_plain<MODE_INT_POLY>(s, pp, d, w, verts, vcap, st, opt.pp_dev); break;
+    case MODE_POLAR_FAST: launch_place_plain<MODE_POLAR_FAST>(s, pp, d, w, verts, vcap, st, opt.pp_dev); break;
 #define CG_PLACE_MODE(MODE)                                                        \
     if (opt.analytic_normals)                                                      \
         launch_place_mode<MODE, true>(s, pp, d, w, verts, vcap, st, opt, et);      \
@@ -493,13 +497,13 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
         CG_CUDA(cudaEventRecord(side->join, side->stream));
         if (opt.qef) CG_TRY(edge_table(&et));
         CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt, et));
-        if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
+        if (ev_after_vertices) CG_CUDA(record_event(ev_after_vertices, st));
         CG_CUDA(cudaStreamWaitEvent(st, side->join, 0));
         return CG_OK;
     }
     if (opt.qef) CG_TRY(edge_table(&et));
     CG_TRY(launch_place(s, su, d, w, verts, vcap, st, opt, et));
-    if (ev_after_vertices) CG_CUDA(cudaEventRecord(ev_after_vertices, st));
+    if (ev_after_vertices) CG_CUDA(record_event(ev_after_vertices, st));
     CG_TRY(launch_quad_count(d, w, st));
     CG_TRY(launch_quad_emit(d, w, idx, icap, st));
     return CG_OK;

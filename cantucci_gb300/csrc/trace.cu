@@ -197,11 +197,13 @@ __global__ void __launch_bounds__(128) k_trace_backward(ShapeDev s, CameraDev c,
             if (v == v && fabsf(v) < 1e30f) acc[k] += v;
         }
     }
+    // per-warp partial sums, added up in a fixed order by k_sum_partials4
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         float v = acc[k];
         for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
-        if ((threadIdx.x & 31) == 0 && v != 0.0f) atomicAdd(&params[k], v);
+        if ((threadIdx.x & 31) == 0) params[4 * w + k] = v;
     }
 }
 
@@ -337,10 +339,15 @@ cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, cons
     cudaStream_t st = (cudaStream_t)stream;
     CG_CUDA(cudaMemsetAsync(grad_params, 0, 4 * sizeof(float), st));
     const uint64_t n = (uint64_t)c.width * c.height;
-    k_trace_backward<<<grid_for(n, 128, 16), 128, 0, st>>>(s, c, dm, depth, grad_depth,
-                                                            grad_params);
-    CG_CHECK_LAUNCH("k_trace_backward");
-    return CG_OK;
+    const unsigned G = grid_for(n, 128, 16);
+    const uint32_t nwarps = G * 4;
+    float* partial = nullptr;
+    CG_CUDA(cudaMallocAsync(&partial, (size_t)nwarps * 4 * sizeof(float), st));
+    k_trace_backward<<<G, 128, 0, st>>>(s, c, dm, depth, grad_depth, partial);
+    cg_status rs = cuda_status(cudaGetLastError(), "k_trace_backward", __FILE__, __LINE__);
+    if (rs == CG_OK) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
+    cudaFreeAsync(partial, st);
+    return rs;
 }
 
 }  // extern "C"

@@ -433,7 +433,8 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
 /* Implicit-surface backward of cg_trace_depth for the polar shape: at a hit
  * x = eye + t d, DE(x; theta) = 0 gives dt/dtheta = -(dDE/dtheta) /
  * (grad_x DE . d).  Sums grad_depth[i] * dt_i/d(power, a, b, c) over hit
- * pixels into grad_params (device, 4 floats).  No reference counterpart. */
+ * pixels into grad_params (device, 4 floats; per-warp partial sums added in
+ * a fixed order, so the result is reproducible).  No reference counterpart. */
 cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, const float* depth,
                             const float* grad_depth, float* grad_params, void* stream);
 
@@ -472,7 +473,8 @@ cg_status cg_de_spatial_grad(const cg_shape* shape, const float* points, uint64_
 /* Backward of DE over a batch (the autograd.Function backward): given the
  * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to
  * grad_points (device n x 3, may be NULL) and the sums over i of
- * g[i] * dDE/d(power, a, b, c) to grad_params (device, 4 floats, may be NULL). */
+ * g[i] * dDE/d(power, a, b, c) to grad_params (device, 4 floats, may be NULL;
+ * summed in a fixed order, so the result is reproducible). */
 cg_status cg_de_backward(const cg_shape* shape, const float* points, const float* grad_out,
                          uint64_t n, float* grad_points, float* grad_params, void* stream);
 
@@ -491,6 +493,9 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
  * "side_stream_priority" (1 default, or 0): whether meshers created
  * afterwards run their quads and copies on a highest-priority stream.
  * "trace_kernel": 1 work-queue march (default), 0 one pixel per thread.
+ * "mesh_graphs" (1 default, or 0): meshes up to resolution 128 (other than
+ * dual contouring) replay a CUDA graph the mesher captured for that
+ * resolution, shape and option set, the span going in as a parameter block.
  * None of these changes an output bit.  "batch_block", "batch_chunk",
  * "batch_brick_min_res", "batch_place_block": the cg_batch_tuning that
  * batches created afterwards start with (defaults 256, 4, 8, 128). */

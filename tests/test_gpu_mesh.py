@@ -445,3 +445,35 @@ def test_launch_knobs_change_no_bit(cg):
         lib.cg_set_option(b"side_stream_priority", 1)
     for v, i in meshes[1:]:
         assert np.array_equal(v, meshes[0][0]) and np.array_equal(i, meshes[0][1])
+
+
+def test_graph_replay_matches_direct_launches(cg):
+    """A mesher replays one captured graph for every span of the same
+    resolution and shape (the span goes in through a parameter block) and
+    captures again when the resolution changes (res 256 is launched
+    directly): each mesh equals the one direct launches give, bit for bit,
+    timings included."""
+    lib = cg.load()
+    s = cg.Mandelbulb(8, 15, 2.5)
+    jobs = [((-1.2, -1.2, -1.2), (0.0, 0.0, 0.0), 32), ((0.0, -1.2, 0.0), (1.2, 0.0, 1.2), 32),
+            ((-0.6, 0.0, -0.6), (0.0, 0.6, 0.0), 32), ((-1.2, -1.2, -1.2), (1.2, 1.2, 1.2), 64),
+            ((0.3, 0.3, -0.9), (0.9, 0.9, -0.3), 32), ((-1.2, -1.2, -1.2), (1.2, 1.2, 1.2), 256),
+            ((-1.2, -1.2, -1.2), (0.0, 0.0, 0.0), 128)]
+    out = {}
+    try:
+        for graphs in (1, 0):
+            assert lib.cg_set_option(b"mesh_graphs", graphs) == 0
+            m = cg.Mesher(0)
+            try:
+                res_list = []
+                for a, b, r in jobs:
+                    v, i, nv, ni, tm = m.generate(cg.Span(a, b), s, r)
+                    assert tm.first_ms > 0 and tm.second_ms > 0
+                    res_list.append((as7(v[:nv]).view(np.uint32).copy(), i[:ni].copy()))
+            finally:
+                m.close()
+            out[graphs] = res_list
+    finally:
+        lib.cg_set_option(b"mesh_graphs", 1)
+    for (va, ia), (vb, ib) in zip(out[1], out[0]):
+        assert len(va) > 0 and np.array_equal(va, vb) and np.array_equal(ia, ib)

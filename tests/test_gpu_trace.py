@@ -126,8 +126,8 @@ def test_fit_reduces_loss(cg):
     p, rot, losses = fit.fit(target, cam, steps=40, lr=1e-2,
                              callback=lambda it, pw, r, l: powers.append(pw))
     # The masked L1 loss is not smooth (the set of pixels hit in both maps
-    # changes with the parameters) and the backward sums with atomics, so
-    # single steps may go up: the bar is on the best step.
+    # changes with the parameters), so single steps may go up: the bar is on
+    # the best step.
     best = int(np.argmin(losses))
     assert losses[best] < 0.95 * losses[0], losses
     power_at = [8.0] + powers  # the callback runs after each step
@@ -191,3 +191,27 @@ def test_fast_march_close_to_exact(cg, orc):
 def W_uniform(n):
     from cantucci_gb300 import workloads as W
     return W.uniform_points(n, seed=41)
+
+
+def test_backward_is_reproducible(cg):
+    """The parameter gradients are summed per warp and then in a fixed order:
+    two backward passes over the same depth map give the same bits (and so
+    a fit is reproducible)."""
+    import ctypes as C
+    import torch
+    from cantucci_gb300 import _ffi, fit
+    lib = _ffi.load()
+    cam = fit.camera(128, 96)
+    shape = cg.MandelbulbPolar(8.3, 15, 2.5, (0.2, 0.1, 0.0))
+    depth = fit.render(8.3, (0.2, 0.1, 0.0), cam)
+    g = torch.randn(depth.shape, device="cuda", generator=torch.Generator("cuda").manual_seed(3))
+    outs = []
+    for _ in range(3):
+        gp = torch.empty(4, device="cuda")
+        st = lib.cg_trace_backward(C.byref(shape._cshape()), C.byref(cam), C.c_void_p(depth.data_ptr()),
+                                   C.c_void_p(g.contiguous().data_ptr()), C.c_void_p(gp.data_ptr()),
+                                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert st == 0
+        torch.cuda.synchronize()
+        outs.append(gp.cpu().numpy().view(np.uint32).copy())
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
