@@ -270,12 +270,15 @@ cg_status enqueue_mesh(cg_mesher* m, const ShapeDev& s, const SpanSetup& su, con
 // (it reads the edge count back mid-way), or capturing failed.
 constexpr uint32_t kGraphMaxRes = 128;
 
+bool graph_sized(const cg_mesher* m, uint32_t res) {
+    return g_mesh_graphs.load() && !m->graph_broken && m->placement != CG_PLACEMENT_QEF &&
+           res <= kGraphMaxRes;
+}
+
 bool launch_mesh_graph(cg_mesher* m, const cg_shape* shape, const ShapeDev& s,
                        const SpanSetup& su, const MeshDims& d, const MeshWork& w,
                        cg_vertex* dverts, uint64_t vcap, uint32_t* didx, uint64_t icap) {
-    if (!g_mesh_graphs.load() || m->graph_broken || m->placement == CG_PLACEMENT_QEF ||
-        d.res > kGraphMaxRes)
-        return false;
+    if (!graph_sized(m, d.res)) return false;
     if (!m->gparams_dev) {
         if (cudaMalloc(&m->gparams_dev, sizeof(MeshGraphParams)) != cudaSuccess ||
             cudaMallocHost(&m->gparams_host, sizeof(MeshGraphParams)) != cudaSuccess) {
@@ -604,9 +607,11 @@ cg_status cg_generate_for_box(cg_mesher* m, const cg_span* span, const cg_shape*
     std::lock_guard<std::mutex> lk(m->mu);
     DeviceGuard g(m->device);
     CG_TRY(check_span_res(span, res));
-    // Pinned outputs: the GPU writes the vertices into them directly and the
-    // index copy overlaps the vertex placement.
-    void* vmap = vertex_cap ? mapped_host(vertices) : nullptr;
+    // Pinned outputs of a mesh too large for a replayed graph: the GPU writes
+    // the vertices into them directly and the index copy overlaps the vertex
+    // placement.  Smaller meshes (and pageable outputs) are meshed into
+    // device staging and copied once the counts are known.
+    void* vmap = vertex_cap && !graph_sized(m, res) ? mapped_host(vertices) : nullptr;
     if (vmap && index_cap && mapped_host(indices)) {
         CG_TRY(run_mesh_to_host(m, span, shape, res, static_cast<cg_vertex*>(vmap), vertex_cap,
                                 indices, index_cap, tm));

@@ -236,11 +236,12 @@ def test_analytic_normals(cg, orc, kind):
         assert np.median(ang_fd) > np.median(ang)
 
 
-@pytest.mark.parametrize("res", [64, 128])
+@pytest.mark.parametrize("res", [64, 128, 256])
 def test_pinned_host_outputs_match_device(cg, mesher, res):
-    """Pinned host outputs take the overlapped path (vertices stored by the
-    GPU straight into host memory, the index copy overlapping placement):
-    same bits as the device-output mesh."""
+    """Pinned host outputs: up to res 128 through device staging and a
+    replayed graph, above it the overlapped path (vertices stored by the GPU
+    straight into host memory, the index copy overlapping placement); same
+    bits as the device-output mesh either way."""
     import torch
     s = cg.Mandelbulb(8, 15, 2.5)
     span = cg.Span(*W.SPAN_C1)
