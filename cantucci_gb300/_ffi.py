@@ -127,6 +127,9 @@ SIGNATURES = [
     ("cg_shape_mesh_focii", _i32, [_vp, _vp, _u32, C.POINTER(_u32)]),
     ("cg_batch_get_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
     ("cg_batch_set_tuning", _i32, [_vp, C.POINTER(CgBatchTuning)]),
+    ("cg_batch_set_normals", _i32, [_vp, _u32]),
+    ("cg_batch_set_numerics", _i32, [_vp, _u32]),
+    ("cg_shape_mesh_set_options", _i32, [_vp, _u32, _u32]),
     ("cg_batch_autotune", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp, _u32,
                                  C.POINTER(CgBatchTuning), C.POINTER(_f32)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),

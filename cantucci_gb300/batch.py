@@ -115,6 +115,18 @@ class BatchMesher:
         t = _ffi.CgBatchTuning(**{**self.tuning, **knobs})
         check(self._lib.cg_batch_set_tuning(self.handle, C.byref(t)))
 
+    def set_normals(self, mode: str):
+        """"fd" (the reference's six-sample difference, default) or
+        "analytic" (one forward-mode pass per vertex)."""
+        modes = {"fd": _ffi.CG_NORMALS_FD, "analytic": _ffi.CG_NORMALS_ADJOINT}
+        check(self._lib.cg_batch_set_normals(self.handle, modes[mode]))
+
+    def set_numerics(self, mode: str):
+        """"exact" (the reference's bits, default) or "fast" (with "fd"
+        normals only)."""
+        modes = {"exact": _ffi.CG_NUMERICS_EXACT, "fast": _ffi.CG_NUMERICS_FAST}
+        check(self._lib.cg_batch_set_numerics(self.handle, modes[mode]))
+
     def tuning_key(self, shape) -> str:
         """Cache key: GPU name and SM count, the shape, the resolutions."""
         torch = _torch()

@@ -96,6 +96,7 @@ struct cg_shape_mesh {
     std::vector<Node> nodes;
     std::vector<Generation> gens;
     cg_batch* batch = nullptr;
+    uint32_t normals = CG_NORMALS_FD, numerics = CG_NUMERICS_EXACT;
     // the run in flight
     bool inflight = false;
     int32_t run_gen = -1;
@@ -263,6 +264,8 @@ cg_status fit_batch(cg_shape_mesh* sm, const std::vector<cg_span_job>& jobs) {
 // Launches the batch into generation `gen` with its current capacities.
 cg_status launch_run(cg_shape_mesh* sm) {
     Generation& g = sm->gens[sm->run_gen];
+    CG_TRY(cg_batch_set_normals(sm->batch, sm->normals));
+    CG_TRY(cg_batch_set_numerics(sm->batch, sm->numerics));
     CG_TRY(cg_batch_mesh(sm->batch, &sm->shape, g.verts, sm->run_vcap, g.idx, sm->run_icap,
                          sm->d_results, sm->d_totals, sm->stream));
     CG_CUDA(cudaMemcpyAsync(sm->h_results, sm->d_results,
@@ -547,6 +550,18 @@ cg_status cg_shape_mesh_focii(cg_shape_mesh* sm, float* points, uint32_t cap, ui
     *count = (uint32_t)(sm->focii.size() / 3);
     for (uint32_t k = 0; k < cap && k < *count; ++k)
         for (int c = 0; c < 3; ++c) points[3 * k + c] = sm->focii[3 * k + c];
+    return CG_OK;
+}
+
+cg_status cg_shape_mesh_set_options(cg_shape_mesh* sm, uint32_t normals, uint32_t numerics) {
+    if (!sm || normals > CG_NORMALS_ADJOINT || numerics > CG_NUMERICS_FAST ||
+        (normals == CG_NORMALS_ADJOINT && numerics == CG_NUMERICS_FAST)) {
+        set_error("bad shape mesh or options (fast numerics with the six-sample normals only)");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(sm->mu);
+    sm->normals = normals;
+    sm->numerics = numerics;
     return CG_OK;
 }
 

@@ -180,7 +180,7 @@ __global__ void k_batch_vertex_list(const BatchJob* __restrict__ jobs, uint32_t 
     }
 }
 
-template <int M>
+template <int M, bool AN>
 __global__ void __launch_bounds__(256) k_batch_place(ShapeDev s, const BatchJob* __restrict__ jobs,
                                                      const float* __restrict__ dists,
                                                      const uint32_t* __restrict__ cellidx,
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) k_batch_place(ShapeDev s, const BatchJob*
     bool bad = false;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const BatchJob& J = jobs[celljob[v]];
-        bad |= !place_vertex<M>(s, J.pp, J.d, dists + J.dist_off, cellidx[v],
+        bad |= !place_vertex<M, AN>(s, J.pp, J.d, dists + J.dist_off, cellidx[v],
                                 reinterpret_cast<float*>(verts + v));
     }
     if (bad) atomicOr(&tot->status, MESH_LERP_FAIL);
@@ -270,6 +270,8 @@ struct cg_batch {
     uint32_t cap_jobs = 0;
     uint64_t cap_dist = 0, cap_sgnw = 0, cap_cw = 0, cap_rows = 0;
     uint32_t plan_gen = 0;  // bumped by cg_batch_set_jobs (graphs recapture)
+    uint32_t normals = CG_NORMALS_FD;       // cg_batch_set_normals
+    uint32_t numerics = CG_NUMERICS_EXACT;  // cg_batch_set_numerics
     // quads are built on `side` beside the vertex placement
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
@@ -402,15 +404,15 @@ cg_status launch_batch_de(cg_batch* b, const ShapeDev& s, cudaStream_t st) {
     return CG_OK;
 }
 
-template <int M>
+template <int M, bool AN = false>
 cg_status launch_batch_place(cg_batch* b, const ShapeDev& s, cg_vertex* vertices,
                              uint64_t vertex_cap, cudaStream_t st) {
     const unsigned B = b->tune.place_block;
     // Eight waves of blocks rather than one resident wave, so that blocks
     // finish throughout the launch (as k_place: measured 10.19 -> 10.02 ms
     // on the 4096-span batch together with the side stream's priority).
-    const unsigned G = resident_grid(k_batch_place<M>, B) * 8;
-    k_batch_place<M><<<G, B, 0, st>>>(s, b->jobs, b->dists, b->cellidx, b->celljob, b->tot,
+    const unsigned G = resident_grid(k_batch_place<M, AN>, B) * 8;
+    k_batch_place<M, AN><<<G, B, 0, st>>>(s, b->jobs, b->dists, b->cellidx, b->celljob, b->tot,
                                       vertices, vertex_cap);
     CG_CHECK_LAUNCH("k_batch_place");
     return CG_OK;
@@ -545,6 +547,26 @@ cg_status cg_batch_set_jobs(cg_batch* b, const cg_span_job* host_jobs, uint32_t 
     return CG_OK;
 }
 
+cg_status cg_batch_set_normals(cg_batch* b, uint32_t normals) {
+    if (!b || normals > CG_NORMALS_ADJOINT) {
+        set_error("bad batch or normals mode");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(b->mu);
+    b->normals = normals;
+    return CG_OK;
+}
+
+cg_status cg_batch_set_numerics(cg_batch* b, uint32_t numerics) {
+    if (!b || numerics > CG_NUMERICS_FAST) {
+        set_error("numerics: CG_NUMERICS_EXACT or CG_NUMERICS_FAST");
+        return CG_EINVAL;
+    }
+    std::lock_guard<std::mutex> lk(b->mu);
+    b->numerics = numerics;
+    return CG_OK;
+}
+
 cg_status cg_batch_get_tuning(const cg_batch* b, cg_batch_tuning* t) {
     if (!b || !t) {
         set_error("bad arguments to cg_batch_get_tuning");
@@ -588,13 +610,24 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
     cudaStream_t st = (cudaStream_t)stream;
     CG_CUDA(cudaMemsetAsync(b->tot, 0, sizeof(BatchTotals), st));
     CG_CUDA(cudaMemsetAsync(b->sgn, 0, b->sgn_words * 4, st));
-    switch (mode_of(s, CG_NUMERICS_EXACT)) {
+    const bool an = b->normals == CG_NORMALS_ADJOINT;
+    if (an && b->numerics == CG_NUMERICS_FAST) {
+        set_error("fast numerics with the six-sample normals only");
+        return CG_EINVAL;
+    }
+    switch (mode_of(s, b->numerics)) {
     case MODE_P8:
         if (p8_unrolled(s)) CG_TRY(launch_batch_de<MODE_P8_IT15>(b, s, st));
         else CG_TRY(launch_batch_de<MODE_P8>(b, s, st));
         break;
     case MODE_INT: CG_TRY(launch_batch_de<MODE_INT>(b, s, st)); break;
     case MODE_POLAR: CG_TRY(launch_batch_de<MODE_POLAR>(b, s, st)); break;
+    case MODE_P8_FAST:
+        if (p8_unrolled(s)) CG_TRY(launch_batch_de<MODE_P8_FAST_IT15>(b, s, st));
+        else CG_TRY(launch_batch_de<MODE_P8_FAST>(b, s, st));
+        break;
+    case MODE_INT_POLY: CG_TRY(launch_batch_de<MODE_INT_POLY>(b, s, st)); break;
+    case MODE_POLAR_FAST: CG_TRY(launch_batch_de<MODE_POLAR_FAST>(b, s, st)); break;
     default: CG_TRY(launch_batch_de<MODE_SPHERE>(b, s, st)); break;
     }
     const unsigned G = grid_for(b->rows, 256, 8);
@@ -620,14 +653,25 @@ cg_status cg_batch_mesh(cg_batch* b, const cg_shape* shape, cg_vertex* vertices,
                                          b->wordoff, b->rowoff, b->quadoff, indices, index_cap);
     CG_CHECK_LAUNCH("k_batch_quad_emit");
     if (b->side) CG_CUDA(cudaEventRecord(b->join, b->side));
-    switch (mode_of(s, CG_NUMERICS_EXACT)) {
-    case MODE_P8:
-        CG_TRY(launch_batch_place<MODE_P8>(b, s, vertices, vertex_cap, st));  // rolled, as k_place
+#define CG_BATCH_PLACE(MODE)                                                      \
+    if (an) CG_TRY((launch_batch_place<MODE, true>(b, s, vertices, vertex_cap, st))); \
+    else CG_TRY((launch_batch_place<MODE, false>(b, s, vertices, vertex_cap, st)));
+    switch (mode_of(s, b->numerics)) {
+    case MODE_P8: CG_BATCH_PLACE(MODE_P8) break;  // rolled, as k_place
+    case MODE_INT: CG_BATCH_PLACE(MODE_INT) break;
+    case MODE_POLAR: CG_BATCH_PLACE(MODE_POLAR) break;
+    case MODE_P8_FAST:
+        CG_TRY((launch_batch_place<MODE_P8_FAST, false>(b, s, vertices, vertex_cap, st)));
         break;
-    case MODE_INT: CG_TRY(launch_batch_place<MODE_INT>(b, s, vertices, vertex_cap, st)); break;
-    case MODE_POLAR: CG_TRY(launch_batch_place<MODE_POLAR>(b, s, vertices, vertex_cap, st)); break;
-    default: CG_TRY(launch_batch_place<MODE_SPHERE>(b, s, vertices, vertex_cap, st)); break;
+    case MODE_INT_POLY:
+        CG_TRY((launch_batch_place<MODE_INT_POLY, false>(b, s, vertices, vertex_cap, st)));
+        break;
+    case MODE_POLAR_FAST:
+        CG_TRY((launch_batch_place<MODE_POLAR_FAST, false>(b, s, vertices, vertex_cap, st)));
+        break;
+    default: CG_BATCH_PLACE(MODE_SPHERE) break;
     }
+#undef CG_BATCH_PLACE
     if (b->side) CG_CUDA(cudaStreamWaitEvent(st, b->join, 0));
     k_batch_results<<<grid_for(b->njobs, 256, 4), 256, 0, st>>>(b->jobs, b->njobs, b->rowoff,
                                                                  b->quadoff, b->tot, results);
@@ -663,6 +707,8 @@ cg_status cg_batch_mesh_graph(cg_batch* b, const cg_shape* shape, cg_vertex* ver
     put(&totals, sizeof totals);
     put(&b->tune, sizeof b->tune);
     put(&b->plan_gen, sizeof b->plan_gen);
+    put(&b->normals, sizeof b->normals);
+    put(&b->numerics, sizeof b->numerics);
     cudaStream_t st = (cudaStream_t)stream;
     if (!b->exec || memcmp(key, b->graph_key, sizeof key) != 0) {
         if (b->exec) {

@@ -110,6 +110,13 @@ class ShapeMesh:
         except Exception:
             pass
 
+    def set_options(self, normals: str = "fd", numerics: str = "exact"):
+        """Normals ("fd" or "analytic") and numerics ("exact" or "fast") of
+        the leaves meshed from the next update on."""
+        nm = {"fd": _ffi.CG_NORMALS_FD, "analytic": _ffi.CG_NORMALS_ADJOINT}[normals]
+        nu = {"exact": _ffi.CG_NUMERICS_EXACT, "fast": _ffi.CG_NUMERICS_FAST}[numerics]
+        check(self._lib.cg_shape_mesh_set_options(self.handle, nm, nu))
+
     def update(self, camera: Camera, wait: bool = False) -> dict:
         st = _ffi.CgLodStats()
         check(self._lib.cg_shape_mesh_update(self.handle, C.byref(camera.to_c()), int(wait),

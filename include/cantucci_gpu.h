@@ -305,6 +305,13 @@ typedef struct cg_batch_tuning {
     uint32_t place_block;
 } cg_batch_tuning;
 
+/* Normals and numerics of the batch's meshes, as cg_mesher_set_normals /
+ * cg_mesher_set_numerics for one span (defaults CG_NORMALS_FD and
+ * CG_NUMERICS_EXACT, the reference's; CG_NUMERICS_FAST only with the
+ * six-sample normals, else cg_batch_mesh fails with CG_EINVAL).  A captured
+ * graph is captured again after a change. */
+cg_status cg_batch_set_normals(cg_batch* batch, uint32_t normals);
+cg_status cg_batch_set_numerics(cg_batch* batch, uint32_t numerics);
 cg_status cg_batch_get_tuning(const cg_batch* batch, cg_batch_tuning* tuning);
 /* Validates (CG_EINVAL) and applies; re-uploads the span table when
  * brick_min_res changes (synchronous).  Not during a cg_batch_mesh capture. */
@@ -409,6 +416,9 @@ cg_status cg_shape_mesh_leaves(cg_shape_mesh* sm, cg_leaf* leaves, uint32_t cap,
 /* The focus points of the last update: hits only, in ray order.  points:
  * HOST, cap x 3 floats; *count = the number of hits. */
 cg_status cg_shape_mesh_focii(cg_shape_mesh* sm, float* points, uint32_t cap, uint32_t* count);
+/* Normals and numerics of the leaves meshed from the next update on (see
+ * cg_batch_set_normals / cg_batch_set_numerics). */
+cg_status cg_shape_mesh_set_options(cg_shape_mesh* sm, uint32_t normals, uint32_t numerics);
 
 /* A pinhole camera: eye looking at target, `up` hint, vertical field of view
  * fov_y (radians), width x height pixels (row-major, row 0 at the top). */

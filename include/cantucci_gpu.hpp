@@ -279,6 +279,12 @@ public:
     ShapeMesh(const ShapeMesh&) = delete;
     ShapeMesh& operator=(const ShapeMesh&) = delete;
 
+    // CG_NORMALS_FD / CG_NORMALS_ADJOINT and CG_NUMERICS_EXACT / CG_NUMERICS_FAST
+    // for the leaves meshed from the next update on.
+    void set_options(uint32_t normals, uint32_t numerics) {
+        check(cg_shape_mesh_set_options(sm_, normals, numerics));
+    }
+
     // ShapeMesh::update; wait = block for the jobs started by earlier updates.
     cg_lod_stats update(const Camera& camera, bool wait = false) {
         const cg_view v = camera.to_c();

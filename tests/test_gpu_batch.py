@@ -175,3 +175,41 @@ def test_tuning_rejects_bad_values(cg):
         with pytest.raises(CantucciError):
             b.set_tuning(**knobs)
     b.close()
+
+
+@pytest.mark.parametrize("normals,numerics", [("analytic", "exact"), ("fd", "fast")])
+def test_batch_options_match_per_span(cg, normals, numerics):
+    """Analytic normals and fast numerics in a batch: every span's mesh is
+    bit-identical to the single-span mesher's under the same option, direct
+    and replayed from a graph (the graph is captured again after the option
+    changes); fast numerics with analytic normals are refused."""
+    from cantucci_gb300.batch import BatchMesher
+    spans, res, _, _ = W.batched_spans(40, seed=21)
+    shape = cg.Mandelbulb(8, 15, 2.5)
+    b = BatchMesher(spans, res)
+    try:
+        b.run(shape, graph=True)  # a graph with the default options first
+        b.set_normals(normals)
+        b.set_numerics(numerics)
+        outs = [b.run(shape), b.run(shape, graph=True)]
+        m = cg.Mesher(0)
+        try:
+            m.set_normals(normals)
+            m.set_numerics(numerics)
+            ref = []
+            for sp, r in zip(spans, res):
+                v, i, nv, ni, _ = m.generate(cg.Span(sp[:3], sp[3:]), shape, int(r), strict=False)
+                ref.append((v[:nv].view(np.float32).reshape(-1, 7).copy(), i[:ni].copy()))
+        finally:
+            m.close()
+        for out in outs:
+            for j in range(len(res)):
+                v, i = out.mesh(j)
+                assert np.array_equal(i, ref[j][1]), j
+                assert np.array_equal(v.view(np.uint32), ref[j][0].view(np.uint32)), j
+        b.set_normals("analytic")
+        b.set_numerics("fast")
+        with pytest.raises(cg.CantucciError):
+            b.run(shape)
+    finally:
+        b.close()

@@ -146,3 +146,35 @@ def test_polar_shape_and_bad_arguments(cg):
     sm.close()
     with pytest.raises(CantucciError):
         ShapeMesh(shape, resolution=48)
+
+
+def test_leaf_options(cg):
+    """Analytic normals for the driver's leaves: every ready leaf equals the
+    single-span mesher with analytic normals, bit for bit; fast numerics
+    with analytic normals are refused."""
+    from cantucci_gb300.lod import Camera
+    shape = cg.Mandelbulb(8, 15, 2.5)
+    sm = make(cg, shape, res=32)
+    sm.set_options(normals="analytic")
+    with pytest.raises(cg.CantucciError):
+        sm.set_options(normals="analytic", numerics="fast")
+    far = Camera(position=(0, -30, 0), direction=(0, 1, 0))
+    sm.update(far, wait=True)
+    sm.update(far, wait=True)
+    m = cg.Mesher(0)
+    m.set_normals("analytic")
+    n = 0
+    try:
+        for leaf in sm.leaves():
+            if not leaf.ready:
+                continue
+            v, i = leaf.mesh()
+            rv, ri, nv, ni, _ = m.generate(cg.Span(leaf.start, leaf.end), shape, 32, strict=False)
+            assert np.array_equal(i, ri[:ni])
+            assert np.array_equal(v.view(np.uint32),
+                                  rv[:nv].view(np.float32).reshape(-1, 7).view(np.uint32))
+            n += 1
+    finally:
+        m.close()
+    assert n == 64
+    sm.close()
