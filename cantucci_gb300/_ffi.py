@@ -9,7 +9,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libcantucci_gpu.so")
+# CANTUCCI_GPU_LIB names another build of the same ABI to load instead (the
+# bounds-checked libcantucci_gpu_checked.so in its tests).
+LIB_PATH = os.environ.get("CANTUCCI_GPU_LIB") or os.path.join(HERE, "_lib", "libcantucci_gpu.so")
 
 CG_OK, CG_EINVAL, CG_ECAPACITY, CG_ELERP, CG_ECUDA, CG_ENOMEM, CG_ETIMEOUT, CG_ENODEV = range(8)
 STATUS_NAMES = {0: "CG_OK", 1: "CG_EINVAL", 2: "CG_ECAPACITY", 3: "CG_ELERP", 4: "CG_ECUDA",
@@ -130,6 +132,7 @@ SIGNATURES = [
     ("cg_batch_set_normals", _i32, [_vp, _u32]),
     ("cg_batch_set_numerics", _i32, [_vp, _u32]),
     ("cg_shape_mesh_set_options", _i32, [_vp, _u32, _u32]),
+    ("cg_debug_oob", _i32, [C.POINTER(_u64), C.POINTER(_u32), _u32]),
     ("cg_batch_autotune", _i32, [_vp, _shp, _vp, _u64, _vp, _u64, _vp, _vp, _vp, _u32,
                                  C.POINTER(CgBatchTuning), C.POINTER(_f32)]),
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),

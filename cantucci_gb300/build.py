@@ -3,6 +3,11 @@
 Every translation unit is compiled for sm_103a only, in parallel, and linked
 into cantucci_gb300/_lib/libcantucci_gpu.so.  Host code is compiled with
 -ffp-contract=off so the span set-up rounds like the reference.
+
+build(checked=True) makes libcantucci_gpu_checked.so instead: the same
+sources with -DCG_CHECKED, where the mesh path's array accesses are bounds
+checked (an out-of-range access is skipped and counted, cg_debug_oob reads
+the count).  It is a test tool, built on demand.
 """
 import concurrent.futures as cf
 import hashlib
@@ -18,6 +23,7 @@ INCLUDE = os.path.join(ROOT, "include")
 LIB_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIB_DIR, "libcantucci_gpu.so")
+CHECKED_LIB = os.path.join(LIB_DIR, "libcantucci_gpu_checked.so")
 
 SOURCES = ["capi.cu", "de_kernels.cu", "mesh.cu", "mesh_batch.cu", "adjoint.cu", "trace.cu", "scan.cu",
            "probe.cu", "noalloc.cu", "lod.cu"]
@@ -34,8 +40,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _inputs_digest() -> str:
+def _inputs_digest(extra=()) -> str:
     h = hashlib.sha256()
+    h.update(" ".join(extra).encode())
     for d in (CSRC, INCLUDE):
         for name in sorted(os.listdir(d)):
             p = os.path.join(d, name)
@@ -48,9 +55,9 @@ def _inputs_digest() -> str:
     return h.hexdigest()
 
 
-def _compile(src: str, verbose: bool) -> str:
-    obj = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", INCLUDE, "-I", CSRC, "-c",
+def _compile(src: str, verbose: bool, obj_dir: str = OBJ_DIR, extra=()) -> str:
+    obj = os.path.join(obj_dir, src.replace(".cu", ".o"))
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC, "-c",
            os.path.join(CSRC, src), "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
@@ -62,27 +69,32 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile (if sources changed) and return the path of the shared library."""
-    digest = _inputs_digest()
-    stamp = os.path.join(LIB_DIR, ".digest")
-    if (not force and os.path.exists(LIB) and os.path.exists(stamp)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    """Compile (if sources changed) and return the path of the shared library
+    (with checked=True, of the bounds-checked variant)."""
+    extra = ("-DCG_CHECKED",) if checked else ()
+    lib = CHECKED_LIB if checked else LIB
+    obj_dir = os.path.join(OBJ_DIR, "checked") if checked else OBJ_DIR
+    digest = _inputs_digest(extra)
+    stamp = os.path.join(LIB_DIR, ".digest_checked" if checked else ".digest")
+    if (not force and os.path.exists(lib) and os.path.exists(stamp)
             and open(stamp).read().strip() == digest):
-        return LIB
-    os.makedirs(OBJ_DIR, exist_ok=True)
+        return lib
+    os.makedirs(obj_dir, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
-    tmp = LIB + ".tmp%d" % os.getpid()
+        objs = list(ex.map(lambda s: _compile(s, verbose, obj_dir, extra), SOURCES))
+    tmp = lib + ".tmp%d" % os.getpid()
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     with open(stamp, "w") as f:
         f.write(digest)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                checked="--checked" in sys.argv))

@@ -705,6 +705,29 @@ cg_status cg_set_option(const char* name, int64_t value) {
     return CG_EINVAL;
 }
 
+cg_status cg_debug_oob(uint64_t* count, uint32_t* line, uint32_t reset) {
+#ifdef CG_CHECKED
+    if (!count || !line) {
+        set_error("NULL argument");
+        return CG_EINVAL;
+    }
+    CG_CUDA(cudaDeviceSynchronize());
+    *count = 0;
+    *line = 0;
+    oob_read_mesh(count, line, reset != 0);
+    oob_read_de_kernels(count, line, reset != 0);
+    oob_read_scan(count, line, reset != 0);
+    oob_read_mesh_batch(count, line, reset != 0);
+    return CG_OK;
+#else
+    (void)count;
+    (void)line;
+    (void)reset;
+    set_error("cg_debug_oob: not the bounds-checked build (libcantucci_gpu_checked.so)");
+    return CG_EINVAL;
+#endif
+}
+
 cg_status cg_mesher_stream(cg_mesher* m, void** stream) {
     if (!m || !stream) {
         set_error("NULL argument");

@@ -35,6 +35,48 @@ inline cg_status cuda_status(cudaError_t e, const char* what, const char* file, 
         if (_st != CG_OK) return _st;                                              \
     } while (0)
 
+// Array accesses of the mesh path: CG_AT(p, i, n) is p[i] for an array of n
+// elements.  In the checked build (-DCG_CHECKED, libcantucci_gpu_checked.so)
+// an index at or past n is not performed: the access goes to a scratch
+// slot, and the translation unit's counters record it (how many, and the
+// source line of the first).  cg_debug_oob() reads and clears them.  No
+// trap, so the context stays usable.
+#ifdef CG_CHECKED
+static __device__ unsigned long long cg_oob_count;
+static __device__ unsigned int cg_oob_line;
+static __device__ unsigned long long cg_oob_sink[8];
+
+template <class T>
+__device__ __forceinline__ T* checked_at(T* p, uint64_t i, uint64_t n, unsigned line) {
+    if (i < n) return p + i;
+    atomicAdd(&cg_oob_count, 1ull);
+    atomicCAS(&cg_oob_line, 0u, line);
+    return reinterpret_cast<T*>(cg_oob_sink);
+}
+#define CG_AT(p, i, n) (*::cg::checked_at((p), (uint64_t)(i), (uint64_t)(n), __LINE__))
+
+// One per translation unit with checked accesses: reads (and with `reset`
+// clears) that unit's counters.
+#define CG_OOB_READER(name)                                                              \
+    void oob_read_##name(uint64_t* count, uint32_t* line, bool reset) {                  \
+        unsigned long long c = 0;                                                        \
+        unsigned int l = 0;                                                              \
+        cudaMemcpyFromSymbol(&c, cg_oob_count, sizeof c);                                \
+        cudaMemcpyFromSymbol(&l, cg_oob_line, sizeof l);                                 \
+        *count += c;                                                                     \
+        if (!*line) *line = l;                                                           \
+        if (reset) {                                                                     \
+            c = 0;                                                                       \
+            l = 0;                                                                       \
+            cudaMemcpyToSymbol(cg_oob_count, &c, sizeof c);                              \
+            cudaMemcpyToSymbol(cg_oob_line, &l, sizeof l);                               \
+        }                                                                                \
+    }
+#else
+#define CG_AT(p, i, n) ((p)[i])
+#define CG_OOB_READER(name)
+#endif
+
 // Number of SMs of the current device (cached per device).
 int sm_count();
 

@@ -9,6 +9,8 @@
 
 namespace cg {
 
+CG_OOB_READER(de_kernels)
+
 template <int M>
 __global__ void __launch_bounds__(256) k_de_points(ShapeDev s, const float* __restrict__ pts,
                                                    uint64_t n, float* __restrict__ out) {
@@ -52,10 +54,10 @@ __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* _
         float x, y, z;
         grid_point(g, i, x, y, z);
         const float d = eval<M>(s, x, y, z);
-        out[i] = d;
+        CG_AT(out, i, total) = d;
         if (sgn && !(__float_as_uint(d) >> 31)) {
             const uint32_t zi = i % g.n, row = i / g.n;
-            atomicOr(&sgn[row * W + (zi >> 5)], 1u << (zi & 31));
+            atomicOr(&CG_AT(sgn, row * W + (zi >> 5), (uint64_t)g.n * g.n * W), 1u << (zi & 31));
         }
     }
 }
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
             bool pos = false;
             if (row_ok && z < n) {
                 const float d = eval<M>(s, px, py, grid_coord(g, 2, z));
-                out[((size_t)x * n + y) * n + z] = d;
+                CG_AT(out, ((size_t)x * n + y) * n + z, (uint64_t)n * n * n) = d;
                 pos = (__float_as_uint(d) >> 31) == 0u;
             }
             if (sgn) {
@@ -108,7 +110,7 @@ __global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
             }
         }
         if (sgn && dz == 0 && row_ok) {
-            uint32_t* wp = &sgn[(x * n + y) * W + ((4 * bz0) >> 5)];
+            uint32_t* wp = &CG_AT(sgn, (x * n + y) * W + ((4 * bz0) >> 5), (uint64_t)n * n * W);
             if (group == 8) *wp = word;
             else if (word) atomicOr(wp, word);
         }

@@ -35,6 +35,13 @@ int set_batch_option(const char* name, int64_t v);
 
 // Step-1 kernel variants (cg_set_option "de_grid_kernel").
 enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3 };
+#ifdef CG_CHECKED
+// Out-of-range counters of each checked translation unit (common.cuh).
+void oob_read_mesh(uint64_t* count, uint32_t* line, bool reset);
+void oob_read_de_kernels(uint64_t* count, uint32_t* line, bool reset);
+void oob_read_scan(uint64_t* count, uint32_t* line, bool reset);
+void oob_read_mesh_batch(uint64_t* count, uint32_t* line, bool reset);
+#endif
 int set_de_grid_kernel(int v);
 int de_grid_kernel_option();
 uint32_t place_blocks_per_sm();

@@ -11,6 +11,8 @@
 
 namespace cg {
 
+CG_OOB_READER(mesh)
+
 MeshDims mesh_dims(uint32_t res) {
     MeshDims d;
     d.res = res;
@@ -60,9 +62,9 @@ __global__ void __launch_bounds__(256) k_sign_words(const float* __restrict__ di
         const uint32_t row = wi / W, w = wi % W;
         const uint32_t z = w * 32 + lane;
         bool pos = false;
-        if (z < n) pos = (__float_as_uint(dists[(size_t)row * n + z]) >> 31) == 0u;
+        if (z < n) pos = (__float_as_uint(CG_AT(dists, (size_t)row * n + z, (uint64_t)n * n * n)) >> 31) == 0u;
         const uint32_t bits = __ballot_sync(0xFFFFFFFFu, pos);
-        if (lane == 0) sgn[wi] = bits;
+        if (lane == 0) CG_AT(sgn, wi, total) = bits;
     }
 }
 
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256) k_cells(const uint32_t* __restrict__ sgn,
     const uint32_t rows = d.res * d.res;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x)
-        rowcnt[r] = cells_row(sgn, d, r, cellbits, wordoff);
+        CG_AT(rowcnt, r, rows) = cells_row(sgn, d, r, cellbits, wordoff);
 }
 
 // Cell index of every vertex, in vertex-id order.
@@ -85,7 +87,8 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
     const uint32_t rows = d.res * d.res;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x)
-        vertex_list_row(d, r, cellbits, wordoff, rowoff[r], ~0ull, cellidx, nullptr, 0);
+        vertex_list_row(d, r, cellbits, wordoff, CG_AT(rowoff, r, rows), (uint64_t)rows * d.res,
+                        cellidx, nullptr, 0);
 }
 
 // One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
@@ -112,21 +115,26 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
          base += gridDim.x * blockDim.x) {
         const uint32_t v = base + lane;
         float o[7] = {0, 0, 0, 0, 0, 0, 0};
-        if (v < V) bad |= !place_vertex<M, AN, ROOT, QEF>(s, pp, d, dists, cellidx[v], o, root_iters, &et);
+        if (v < V)
+            bad |= !place_vertex<M, AN, ROOT, QEF>(s, pp, d, dists,
+                                                   CG_AT(cellidx, v, (uint64_t)d.res * d.res * d.res),
+                                                   o, root_iters, &et);
 #pragma unroll
         for (int k = 0; k < 7; ++k) st[lane * 7 + k] = o[k];
         __syncwarp();
         const uint64_t room = base < vcap ? vcap - base : 0;
         uint32_t nw = V - base < 32u ? V - base : 32u;
         if ((uint64_t)nw > room) nw = (uint32_t)room;
-        float* dst = reinterpret_cast<float*>(verts + base);
         if (nw == 32 && vec_ok) {
+            // 32 vertices from base (a multiple of 32): float4 units from base * 7 / 4
             const float4* src4 = reinterpret_cast<const float4*>(st);
-            float4* dst4 = reinterpret_cast<float4*>(dst);
-            dst4[lane] = src4[lane];
-            if (lane < 24) dst4[32 + lane] = src4[32 + lane];
+            float4* v4 = reinterpret_cast<float4*>(verts);
+            const uint64_t b4 = (uint64_t)base * 7 / 4, n4 = vcap * 7 / 4;
+            CG_AT(v4, b4 + lane, n4) = src4[lane];
+            if (lane < 24) CG_AT(v4, b4 + 32 + lane, n4) = src4[32 + lane];
         } else {
-            for (uint32_t i = lane; i < nw * 7; i += 32) dst[i] = st[i];
+            float* vf = reinterpret_cast<float*>(verts);
+            for (uint32_t i = lane; i < nw * 7; i += 32) CG_AT(vf, (uint64_t)base * 7 + i, vcap * 7) = st[i];
         }
         __syncwarp();
     }
@@ -144,10 +152,10 @@ __global__ void __launch_bounds__(256) k_edge_rows(const uint32_t* __restrict__ 
         const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
         uint32_t run = 0;
         for (uint32_t w = 0; w < d.W; ++w) {
-            ewoff[r * d.W + w] = run;
+            CG_AT(ewoff, r * d.W + w, (uint64_t)rows * d.W) = run;
             run += __popc(edge_bits(sgn, d, a, x, y, w));
         }
-        ecount[r] = run;
+        CG_AT(ecount, r, rows) = run;
     }
 }
 
@@ -155,18 +163,18 @@ __global__ void __launch_bounds__(256) k_edge_rows(const uint32_t* __restrict__ 
 __global__ void __launch_bounds__(256) k_edge_list(const uint32_t* __restrict__ sgn, MeshDims d,
                                                    const uint32_t* __restrict__ eoff,
                                                    const uint32_t* __restrict__ ewoff,
-                                                   uint32_t* __restrict__ list) {
+                                                   uint32_t* __restrict__ list, uint32_t E) {
     const uint32_t n2 = d.n * d.n, rows = 3 * n2;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x) {
         const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
         for (uint32_t w = 0; w < d.W; ++w) {
             uint32_t bits = edge_bits(sgn, d, a, x, y, w);
-            uint32_t v = eoff[r] + ewoff[r * d.W + w];
+            uint32_t v = CG_AT(eoff, r, rows) + CG_AT(ewoff, r * d.W + w, (uint64_t)rows * d.W);
             while (bits) {
                 const uint32_t b = __ffs(bits) - 1;
                 bits &= bits - 1;
-                list[v++] = r * d.n + w * 32 + b;
+                CG_AT(list, v++, E) = r * d.n + w * 32 + b;
             }
         }
     }
@@ -183,12 +191,12 @@ __global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, M
                                                    float4* __restrict__ data, uint32_t root_iters) {
     const uint32_t E = cnt->edges, n2 = d.n * d.n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
-        const uint32_t code = list[i];
+        const uint32_t code = CG_AT(list, i, E);
         const uint32_t z = code % d.n, r = code / d.n;
         const uint32_t a = r / n2, row = r % n2, x = row / d.n, y = row % d.n;
         const uint32_t x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
-        const float f0 = dists[((size_t)x * d.n + y) * d.n + z];
-        const float f1 = dists[((size_t)x1 * d.n + y1) * d.n + z1];
+        const float f0 = CG_AT(dists, ((size_t)x * d.n + y) * d.n + z, (uint64_t)d.n * d.n * d.n);
+        const float f1 = CG_AT(dists, ((size_t)x1 * d.n + y1) * d.n + z1, (uint64_t)d.n * d.n * d.n);
         const float ax = __fadd_rn(pp.start[0], __fmul_rn((float)x, pp.step[0]));
         const float ay = __fadd_rn(pp.start[1], __fmul_rn((float)y, pp.step[1]));
         const float az = __fadd_rn(pp.start[2], __fmul_rn((float)z, pp.step[2]));
@@ -204,7 +212,7 @@ __global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, M
         // edge's axis).
         float g[4];
         shape_gradient<M>(s, __fmaf_rn(t, ex, ax), __fmaf_rn(t, ey, ay), __fmaf_rn(t, ez, az), g);
-        data[i] = make_float4(t, g[1], g[2], g[3]);
+        CG_AT(data, i, E) = make_float4(t, g[1], g[2], g[3]);
     }
 }
 
@@ -213,7 +221,7 @@ __global__ void __launch_bounds__(256) k_quad_count(const uint32_t* __restrict__
     const uint32_t rows = d.res * d.res;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x)
-        quadcnt[r] = quad_count_row(sgn, d, r);
+        CG_AT(quadcnt, r, rows) = quad_count_row(sgn, d, r);
 }
 
 __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ sgn, MeshDims d,
@@ -226,7 +234,8 @@ __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ 
     const uint32_t rows = d.res * d.res;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x)
-        quad_emit_row(sgn, d, dists, cellbits, wordoff, rowoff, 0u, quadoff[r], idx, icap, r);
+        quad_emit_row(sgn, d, dists, cellbits, wordoff, rowoff, 0u, CG_AT(quadoff, r, rows), idx,
+                      icap, r);
 }
 
 __global__ void __launch_bounds__(256) k_points_table(MeshDims d,
@@ -238,8 +247,8 @@ __global__ void __launch_bounds__(256) k_points_table(MeshDims d,
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < total;
          c += gridDim.x * blockDim.x) {
         const uint32_t z = c % d.res, r = c / d.res;
-        const uint32_t word = cellbits[r * d.Wc + (z >> 5)];
-        points[c] = ((word >> (z & 31)) & 1u)
+        const uint32_t word = CG_AT(cellbits, r * d.Wc + (z >> 5), (uint64_t)d.res * d.res * d.Wc);
+        CG_AT(points, c, total) = ((word >> (z & 31)) & 1u)
                         ? vertex_id(d, cellbits, wordoff, rowoff, r / d.res, r % d.res, z)
                         : 0xFFFFFFFFu;
     }
@@ -361,7 +370,7 @@ static cg_status launch_edge_data(const ShapeDev& s, const PlaceParams& pp, cons
     {
         const uint32_t rows = 3 * d.n * d.n;
         const unsigned B = 256, G = grid_for(rows, B, 8);
-        k_edge_list<<<G, B, 0, st>>>(w.sgn, d, e.eoff, e.ewoff, list);
+        k_edge_list<<<G, B, 0, st>>>(w.sgn, d, e.eoff, e.ewoff, list, E);
         CG_CHECK_LAUNCH("k_edge_list");
     }
     const unsigned B = 128, G = (unsigned)sm_count() * 16;
@@ -383,6 +392,7 @@ static cg_status launch_edge_data(const ShapeDev& s, const PlaceParams& pp, cons
     et->eoff = e.eoff;
     et->ewoff = e.ewoff;
     et->data = data;
+    et->edges = E;
     return CG_OK;
 }
 

@@ -35,6 +35,8 @@
 
 namespace cg {
 
+CG_OOB_READER(mesh_batch)
+
 struct BatchJob {
     float start[3], across[3];  // widened span (buffer.rs:64-67,77)
     float inv_res;

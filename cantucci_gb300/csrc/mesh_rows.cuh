@@ -29,10 +29,10 @@ __device__ __forceinline__ uint32_t valid_mask(uint32_t res, uint32_t w) {
 }
 
 // Sign word of corner row `row` shifted by one corner: bit b = corner 32w+b+1.
-__device__ __forceinline__ uint32_t sign_hi(const uint32_t* __restrict__ sgn, uint32_t row,
-                                            uint32_t W, uint32_t w) {
-    const uint32_t lo = sgn[row * W + w];
-    const uint32_t nx = (w + 1 < W) ? sgn[row * W + w + 1] : 0u;
+__device__ __forceinline__ uint32_t sign_hi(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                            uint32_t row, uint32_t w) {
+    const uint32_t lo = CG_AT(sgn, row * d.W + w, (uint64_t)d.n * d.n * d.W);
+    const uint32_t nx = (w + 1 < d.W) ? CG_AT(sgn, row * d.W + w + 1, (uint64_t)d.n * d.n * d.W) : 0u;
     return (lo >> 1) | (nx << 31);
 }
 
@@ -45,15 +45,16 @@ __device__ __forceinline__ uint32_t cells_row(const uint32_t* __restrict__ sgn, 
     const uint32_t r00 = x * d.n + y, r01 = r00 + 1, r10 = r00 + d.n, r11 = r10 + 1;
     uint32_t run = 0;
     for (uint32_t w = 0; w < d.Wc; ++w) {
-        const uint32_t a0 = sgn[r00 * d.W + w], a1 = sgn[r01 * d.W + w];
-        const uint32_t a2 = sgn[r10 * d.W + w], a3 = sgn[r11 * d.W + w];
-        const uint32_t b0 = sign_hi(sgn, r00, d.W, w), b1 = sign_hi(sgn, r01, d.W, w);
-        const uint32_t b2 = sign_hi(sgn, r10, d.W, w), b3 = sign_hi(sgn, r11, d.W, w);
+        const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+        const uint32_t a0 = CG_AT(sgn, r00 * d.W + w, ns), a1 = CG_AT(sgn, r01 * d.W + w, ns);
+        const uint32_t a2 = CG_AT(sgn, r10 * d.W + w, ns), a3 = CG_AT(sgn, r11 * d.W + w, ns);
+        const uint32_t b0 = sign_hi(sgn, d, r00, w), b1 = sign_hi(sgn, d, r01, w);
+        const uint32_t b2 = sign_hi(sgn, d, r10, w), b3 = sign_hi(sgn, d, r11, w);
         const uint32_t all1 = a0 & a1 & a2 & a3 & b0 & b1 & b2 & b3;
         const uint32_t any1 = a0 | a1 | a2 | a3 | b0 | b1 | b2 | b3;
         const uint32_t surf = any1 & ~all1 & valid_mask(d.res, w);
-        cellbits[r * d.Wc + w] = surf;
-        wordoff[r * d.Wc + w] = run;
+        CG_AT(cellbits, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc) = surf;
+        CG_AT(wordoff, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc) = run;
         run += __popc(surf);
     }
     return run;
@@ -68,14 +69,14 @@ __device__ __forceinline__ void vertex_list_row(const MeshDims& d, uint32_t r,
                                                 uint64_t cap, uint32_t* __restrict__ cellidx,
                                                 uint32_t* __restrict__ tag, uint32_t tag_value) {
     for (uint32_t w = 0; w < d.Wc; ++w) {
-        uint32_t bits = cellbits[r * d.Wc + w];
-        uint32_t v = base + wordoff[r * d.Wc + w];
+        uint32_t bits = CG_AT(cellbits, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc);
+        uint32_t v = base + CG_AT(wordoff, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc);
         while (bits) {
             const uint32_t b = __ffs(bits) - 1;
             bits &= bits - 1;
             if (v < cap) {
-                cellidx[v] = r * d.res + w * 32 + b;
-                if (tag) tag[v] = tag_value;
+                CG_AT(cellidx, v, cap) = r * d.res + w * 32 + b;
+                if (tag) CG_AT(tag, v, cap) = tag_value;
             }
             ++v;
         }
@@ -111,16 +112,18 @@ struct EdgeTable {
     const uint32_t* eoff;   // edges before row r (3 n^2)
     const uint32_t* ewoff;  // edges before word w within row r (3 n^2 W)
     const float4* data;     // per edge: t, gradient
+    uint32_t edges;         // entries of data
 };
 
 // Sign-change bits of the axis-a edges of corner row (x, y), word w.
 __device__ __forceinline__ uint32_t edge_bits(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                               uint32_t a, uint32_t x, uint32_t y, uint32_t w) {
     const uint32_t row = x * d.n + y;
-    const uint32_t base = sgn[row * d.W + w];
-    if (a == 0) return x + 1 < d.n ? base ^ sgn[(row + d.n) * d.W + w] : 0u;
-    if (a == 1) return y + 1 < d.n ? base ^ sgn[(row + 1) * d.W + w] : 0u;
-    return (base ^ sign_hi(sgn, row, d.W, w)) & valid_mask(d.res, w);
+    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    const uint32_t base = CG_AT(sgn, row * d.W + w, ns);
+    if (a == 0) return x + 1 < d.n ? base ^ CG_AT(sgn, (row + d.n) * d.W + w, ns) : 0u;
+    if (a == 1) return y + 1 < d.n ? base ^ CG_AT(sgn, (row + 1) * d.W + w, ns) : 0u;
+    return (base ^ sign_hi(sgn, d, row, w)) & valid_mask(d.res, w);
 }
 
 // The reference's crossing on edge (from, to) of a cell with first corner
@@ -230,7 +233,7 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const uint32_t cx = x + ((k >> 2) & 1), cy = y + ((k >> 1) & 1), cz = z + (k & 1);
-        dd[k] = dists[((size_t)cx * d.n + cy) * d.n + cz];
+        dd[k] = CG_AT(dists, ((size_t)cx * d.n + cy) * d.n + cz, (uint64_t)d.n * d.n * d.n);
     }
     const float p0x = __fadd_rn(pp.start[0], __fmul_rn((float)x, pp.step[0]));
     const float p0y = __fadd_rn(pp.start[1], __fmul_rn((float)y, pp.step[1]));
@@ -289,8 +292,10 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
             const uint32_t w = cz >> 5, b = cz & 31;
             const uint32_t r = a * d.n * d.n + cx * d.n + cy;
             const uint32_t bits = edge_bits(et->sgn, d, a, cx, cy, w);
-            const uint32_t id = et->eoff[r] + et->ewoff[r * d.W + w] + __popc(bits & ((1u << b) - 1u));
-            const float4 e = et->data[id];
+            const uint64_t nr = 3ull * d.n * d.n;
+            const uint32_t id = CG_AT(et->eoff, r, nr) + CG_AT(et->ewoff, r * d.W + w, nr * d.W) +
+                                __popc(bits & ((1u << b) - 1u));
+            const float4 e = CG_AT(et->data, id, et->edges);
             float rx = ((from >> 2) & 1) ? pp.step[0] : 0.0f;
             float ry = ((from >> 1) & 1) ? pp.step[1] : 0.0f;
             float rz = (from & 1) ? pp.step[2] : 0.0f;
@@ -376,13 +381,14 @@ struct EdgeWords {
 __device__ __forceinline__ EdgeWords edge_words(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                                 uint32_t x, uint32_t y, uint32_t w) {
     const uint32_t r = x * d.n + y;
-    const uint32_t base = sgn[r * d.W + w];
+    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    const uint32_t base = CG_AT(sgn, r * d.W + w, ns);
     const uint32_t valid = valid_mask(d.res, w);
     const uint32_t zpos = valid & (w == 0 ? ~1u : ~0u);
     EdgeWords e;
-    e.ex = (y > 0) ? ((base ^ sgn[(r + d.n) * d.W + w]) & zpos) : 0u;
-    e.ey = (x > 0) ? ((base ^ sgn[(r + 1) * d.W + w]) & zpos) : 0u;
-    e.ez = (x > 0 && y > 0) ? ((base ^ sign_hi(sgn, r, d.W, w)) & valid) : 0u;
+    e.ex = (y > 0) ? ((base ^ CG_AT(sgn, (r + d.n) * d.W + w, ns)) & zpos) : 0u;
+    e.ey = (x > 0) ? ((base ^ CG_AT(sgn, (r + 1) * d.W + w, ns)) & zpos) : 0u;
+    e.ez = (x > 0 && y > 0) ? ((base ^ sign_hi(sgn, d, r, w)) & valid) : 0u;
     return e;
 }
 
@@ -402,7 +408,9 @@ __device__ __forceinline__ uint32_t vertex_id(const MeshDims& d, const uint32_t*
                                               const uint32_t* __restrict__ rowoff, uint32_t x,
                                               uint32_t y, uint32_t z) {
     const uint32_t r = x * d.res + y, w = z >> 5, b = z & 31;
-    return rowoff[r] + wordoff[r * d.Wc + w] + __popc(cellbits[r * d.Wc + w] & ((1u << b) - 1u));
+    const uint64_t nc = (uint64_t)d.res * d.res * d.Wc;
+    return CG_AT(rowoff, r, (uint64_t)d.res * d.res) + CG_AT(wordoff, r * d.Wc + w, nc) +
+           __popc(CG_AT(cellbits, r * d.Wc + w, nc) & ((1u << b) - 1u));
 }
 
 // Quad indices of corner row r (buffer.rs:288-372): corner order, then +x,
@@ -423,7 +431,7 @@ __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, 
             const uint32_t b = __ffs(any) - 1;
             any &= any - 1;
             const uint32_t z = w * 32 + b;
-            const bool neg = dists[((size_t)x * d.n + y) * d.n + z] < 0.0f;
+            const bool neg = CG_AT(dists, ((size_t)x * d.n + y) * d.n + z, (uint64_t)d.n * d.n * d.n) < 0.0f;
             const uint32_t bit = 1u << b;
             uint32_t t[6];
             if (e.ex & bit) {
@@ -434,7 +442,7 @@ __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, 
                 if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
                 else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
                 if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
                 ++q;
             }
             if (e.ey & bit) {
@@ -445,7 +453,7 @@ __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, 
                 if (neg) { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
                 else     { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
                 if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
                 ++q;
             }
             if (e.ez & bit) {
@@ -456,7 +464,7 @@ __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, 
                 if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
                 else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
                 if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) idx[6 * q + k] = t[k];
+                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
                 ++q;
             }
         }

@@ -10,6 +10,8 @@
 
 namespace cg {
 
+CG_OOB_READER(scan)
+
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
@@ -53,10 +55,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k)
-        if (base + k < n) s += in[base + k];
+        if (base + k < n) s += CG_AT(in, base + k, n);
     uint32_t total;
     block_exclusive_scan(s, ws, total);
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+    if (threadIdx.x == 0) CG_AT(tile_sums, blockIdx.x, gridDim.x) = total;
 }
 
 // One CTA: exclusive scan of the tile sums in place, total to *total.
@@ -68,14 +70,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(uint32_t* __restrict_
     uint32_t v[SCAN_ITEMS], s = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        v[k] = (base + k < ntiles) ? tile_sums[base + k] : 0;
+        v[k] = (base + k < ntiles) ? CG_AT(tile_sums, base + k, ntiles) : 0;
         s += v[k];
     }
     uint32_t tot;
     uint32_t off = block_exclusive_scan(s, ws, tot);
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        if (base + k < ntiles) tile_sums[base + k] = off;
+        if (base + k < ntiles) CG_AT(tile_sums, base + k, ntiles) = off;
         off += v[k];
     }
     if (threadIdx.x == 0) *total = tot;
@@ -90,14 +92,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
     uint32_t v[SCAN_ITEMS], s = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        v[k] = (base + k < n) ? in[base + k] : 0;
+        v[k] = (base + k < n) ? CG_AT(in, base + k, n) : 0;
         s += v[k];
     }
     uint32_t tot;
     uint32_t off = block_exclusive_scan(s, ws, tot) + tile_off[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        if (base + k < n) out[base + k] = off;
+        if (base + k < n) CG_AT(out, base + k, n) = off;
         off += v[k];
     }
 }

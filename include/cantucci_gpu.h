@@ -511,6 +511,13 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
  * batches created afterwards start with (defaults 256, 4, 8, 128). */
 cg_status cg_set_option(const char* name, int64_t value);
 
+/* The bounds-checked build (libcantucci_gpu_checked.so, built with
+ * -DCG_CHECKED): the number of out-of-range array accesses the mesh path's
+ * kernels skipped since the last reset, and the source line of the first
+ * (0 if none).  Synchronises the device; reset != 0 clears the counts.  In
+ * the normal build it fails with CG_EINVAL. */
+cg_status cg_debug_oob(uint64_t* count, uint32_t* line, uint32_t reset);
+
 /* The cudaStream_t (as void*) the mesher launches on, so a caller can time
  * its calls with CUDA events on that stream. */
 cg_status cg_mesher_stream(cg_mesher* mesher, void** stream);
