@@ -87,8 +87,12 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
     const uint32_t rows = d.res * d.res;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
          r += gridDim.x * blockDim.x)
+#ifdef CG_CHECKED
         vertex_list_row(d, r, cellbits, wordoff, CG_AT(rowoff, r, rows), (uint64_t)rows * d.res,
                         cellidx, nullptr, 0);
+#else
+        vertex_list_row(d, r, cellbits, wordoff, rowoff[r], ~0ull, cellidx, nullptr, 0);
+#endif
 }
 
 // One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
@@ -126,12 +130,18 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
         uint32_t nw = V - base < 32u ? V - base : 32u;
         if ((uint64_t)nw > room) nw = (uint32_t)room;
         if (nw == 32 && vec_ok) {
-            // 32 vertices from base (a multiple of 32): float4 units from base * 7 / 4
+            // 32 vertices from base (a multiple of 32) = 56 float4 units
             const float4* src4 = reinterpret_cast<const float4*>(st);
+#ifdef CG_CHECKED
             float4* v4 = reinterpret_cast<float4*>(verts);
             const uint64_t b4 = (uint64_t)base * 7 / 4, n4 = vcap * 7 / 4;
             CG_AT(v4, b4 + lane, n4) = src4[lane];
             if (lane < 24) CG_AT(v4, b4 + 32 + lane, n4) = src4[32 + lane];
+#else
+            float4* dst4 = reinterpret_cast<float4*>(verts + base);
+            dst4[lane] = src4[lane];
+            if (lane < 24) dst4[32 + lane] = src4[32 + lane];
+#endif
         } else {
             float* vf = reinterpret_cast<float*>(verts);
             for (uint32_t i = lane; i < nw * 7; i += 32) CG_AT(vf, (uint64_t)base * 7 + i, vcap * 7) = st[i];
