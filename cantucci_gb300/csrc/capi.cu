@@ -612,9 +612,10 @@ cg_status cg_generate_for_box(cg_mesher* m, const cg_span* span, const cg_shape*
     // placement.  Smaller meshes (and pageable outputs) are meshed into
     // device staging and copied once the counts are known.
     void* vmap = vertex_cap && !graph_sized(m, res) ? mapped_host(vertices) : nullptr;
-    if (vmap && index_cap && mapped_host(indices)) {
+    void* imap = vmap && index_cap ? mapped_host(indices) : nullptr;
+    if (vmap && imap) {
         CG_TRY(run_mesh_to_host(m, span, shape, res, static_cast<cg_vertex*>(vmap), vertex_cap,
-                                indices, index_cap, tm));
+                                static_cast<uint32_t*>(imap), index_cap, tm));
         const MeshCounters c = *m->hcnt;
         if (n_vertices) *n_vertices = c.vertices;
         if (n_indices) *n_indices = 6ull * c.quads;

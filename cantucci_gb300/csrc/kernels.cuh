@@ -146,9 +146,10 @@ cg_status launch_mesh_from_dists(const ShapeDev& s, const SpanSetup& su, const M
 // The same steps for a mesh whose outputs go to host memory, reordered so
 // the transfers overlap the vertex placement: surface cells and both counts
 // first (read back: ev_counts is synchronised), then the quad indices into
-// `dev_idx` and their device-to-host copy on `copy_st` (ev_quads marks the
+// `dev_idx` and their copy to `host_idx` on `copy_st` (ev_quads marks the
 // end of the indices), while on `st` k_place stores the vertices straight
-// into `host_verts` (pinned, device-mapped).
+// into `host_verts`.  Both host buffers are pinned and passed by their
+// device-mapped addresses.
 cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const MeshDims& d,
                               const MeshWork& w, cg_vertex* host_verts, uint64_t vcap,
                               uint32_t* dev_idx, uint32_t* host_idx, uint64_t icap,

@@ -248,6 +248,24 @@ __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ 
                       icap, r);
 }
 
+// Copy of the first n words of src (n <= src_cap) to dst (n <= dst_cap),
+// both 16-byte aligned, as 16-byte units: the quad indices into mapped host
+// memory.  A few blocks keep the link busy; beside the placement they cost
+// less than a copy-engine transfer, whose traffic competes with the
+// placement's own stores into host memory.
+static constexpr unsigned kCopyBlocks = 16;
+
+__global__ void __launch_bounds__(256) k_copy_words(const uint32_t* __restrict__ src,
+                                                    uint64_t src_cap, uint32_t* __restrict__ dst,
+                                                    uint64_t dst_cap, uint64_t n) {
+    const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (uint64_t i = t; i < n4; i += stride) CG_AT(d4, i, dst_cap / 4) = CG_AT(s4, i, src_cap / 4);
+    for (uint64_t i = n4 * 4 + t; i < n; i += stride) CG_AT(dst, i, dst_cap) = CG_AT(src, i, src_cap);
+}
+
 __global__ void __launch_bounds__(256) k_points_table(MeshDims d,
                                                      const uint32_t* __restrict__ cellbits,
                                                      const uint32_t* __restrict__ wordoff,
@@ -547,9 +565,13 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     CG_CUDA(cudaStreamWaitEvent(copy_st, ev_counts, 0));
     CG_TRY(launch_quad_emit(d, w, dev_idx, icap, copy_st));
     CG_CUDA(cudaEventRecord(ev_quads, copy_st));
-    if (ci)
+    if (ci && (((uintptr_t)host_idx | (uintptr_t)dev_idx) & 15u) == 0u) {
+        k_copy_words<<<kCopyBlocks, 256, 0, copy_st>>>(dev_idx, icap, host_idx, icap, ci);
+        CG_CHECK_LAUNCH("k_copy_words");
+    } else if (ci) {
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                                 copy_st));
+    }
     EdgeTable et{};
     if (opt.qef) CG_TRY(launch_edge_data(s, place_params(su), d, w, opt, hcnt->edges, st, &et));
     CG_TRY(launch_place(s, su, d, w, host_verts, vcap, st, opt, et));

@@ -260,6 +260,33 @@ def test_pinned_host_outputs_match_device(cg, mesher, res):
     assert tm.first_ms > 0 and tm.second_ms > 0 and tm.third_ms > 0
 
 
+@pytest.mark.parametrize("offset", [1, 2, 4])
+def test_pinned_host_outputs_offset_buffers(cg, mesher, offset):
+    """The overlapped path copies the indices with a kernel in 16-byte units
+    when both buffers are 16-byte aligned (offset 4 words), else with a
+    copy-engine transfer (offsets 1 and 2); index counts 6q leave a 2-word
+    tail when q is odd.  Same words either way, nothing written past them."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    res = 256
+    vcap, icap = res ** 3 // 8, 18 * res ** 3 // 8
+    v = torch.empty((vcap, 7), dtype=torch.float32, device="cuda")
+    i = torch.empty(icap, dtype=torch.int32, device="cuda")
+    nv, ni, _ = mesher.generate_device(span, s, res, v, i)
+    vh = torch.zeros((vcap, 7), dtype=torch.float32, pin_memory=True)
+    ih = torch.full((icap + offset + 8,), -7, dtype=torch.int32, pin_memory=True)
+    inp = ih.numpy().view(np.uint32)[offset:offset + icap]
+    _, _, nv2, ni2, _ = mesher.generate(span, s, res,
+                                        vertices=vh.numpy().view(cg.VERTEX_DTYPE).reshape(-1),
+                                        indices=inp)
+    assert (nv2, ni2) == (nv, ni)
+    got = ih.numpy()
+    assert np.array_equal(got[offset:offset + ni], i[:ni].cpu().numpy())
+    assert np.all(got[:offset] == -7) and np.all(got[offset + ni:] == -7)
+    assert np.array_equal(vh[:nv].numpy().view(np.uint32), v[:nv].cpu().numpy().view(np.uint32))
+
+
 def test_pinned_host_outputs_capacity(cg, mesher):
     """Too-small pinned outputs: CG_ECAPACITY with the full counts, and the
     prefix that fits is the mesh's."""
