@@ -188,7 +188,11 @@ cg_status cg_mesher_set_numerics(cg_mesher* mesher, uint32_t numerics);
 /* MeshBuffer::generate_for_box (src/mesh/buffer.rs:30-42) into HOST buffers.
  * Writes min(count, cap) items; if a count exceeds its capacity the call
  * returns CG_ECAPACITY with *n_vertices / *n_indices set to the required
- * counts.  timings may be NULL. */
+ * counts.  timings may be NULL.  Page-locked (cudaHostAlloc / pinned)
+ * outputs of meshes above resolution 128 are written by the GPU itself: the
+ * vertices by the placement kernel, the indices by a copy beside it (a
+ * kernel when both buffers are 16-byte aligned).  Smaller meshes and
+ * pageable outputs are meshed into device staging and copied. */
 cg_status cg_generate_for_box(cg_mesher* mesher, const cg_span* span, const cg_shape* shape,
                               uint32_t resolution, cg_vertex* vertices, uint64_t vertex_cap,
                               uint32_t* indices, uint64_t index_cap, uint64_t* n_vertices,
