@@ -100,9 +100,8 @@ __device__ __forceinline__ void polar_step_deriv(const ShapeDev& s, float qx, fl
 
 __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __restrict__ dm,
                                               float px, float py, float pz, float* out) {
-    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-    const float qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    float qx, qy, qz;
+    rotate_point(s, px, py, pz, qx, qy, qz);
     const float P = s.power_f;
     const uint32_t N = s.max_iters;
 
@@ -226,15 +225,7 @@ template <int T, bool Rot = true, bool FAST = false>
 __device__ __forceinline__ void polar_de_tangent(const ShapeDev& s, const float* __restrict__ dm,
                                                  float px, float py, float pz, float* out) {
     float qx, qy, qz;
-    if (FAST) {
-        qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
-        qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
-        qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
-    } else {
-        qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-        qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-        qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
-    }
+    rotate_point<FAST>(s, px, py, pz, qx, qy, qz);
     const float P = s.power_f;
     float zx = qx, zy = qy, zz = qz, dr = 1.0f, r = 0.0f;
     // tangents: direction k has (tx, ty, tz, tdr); dq_k = e_k for k < 3

@@ -57,6 +57,7 @@ __host__ ShapeDev make_shape_dev(const cg_shape& s) {
     for (int i = 0; i < 9; ++i) d.m[i] = (float)m[i];
     for (int i = 0; i < 3; ++i) d.center[i] = s.center[i];
     d.radius = s.radius;
+    d.rotated = s.rot[0] != 0.0f || s.rot[1] != 0.0f || s.rot[2] != 0.0f;
     return d;
 }
 

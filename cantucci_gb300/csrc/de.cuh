@@ -26,6 +26,7 @@ struct ShapeDev {
     float m[9];        // row-major R; the DE is evaluated at R^T p
     float center[3];
     float radius;
+    int32_t rotated;   // 0 when all three Euler angles are 0: q = p exactly
 };
 
 __host__ ShapeDev make_shape_dev(const cg_shape& s);
@@ -36,6 +37,28 @@ __host__ ShapeDev make_shape_dev(const cg_shape& s);
 // canonical NaN is positive; outputs are mapped to the x86 pattern.
 __device__ __forceinline__ float x86_nan(float v) {
     return (v != v) ? __uint_as_float(0xFFC00000u) : v;
+}
+
+// q = R^T p for the polar form, one rounding per operation, sums left to
+// right (FMA = true: the contracted form of the fast paths).  Without a
+// rotation q = p, as in src/shape/mandelbulb.frag, which applies none: signed
+// zeros and non-finite coordinates pass unchanged.
+template <bool FMA = false>
+__device__ __forceinline__ void rotate_point(const ShapeDev& s, float px, float py, float pz,
+                                             float& qx, float& qy, float& qz) {
+    if (!s.rotated) {
+        qx = px;
+        qy = py;
+        qz = pz;
+    } else if (FMA) {
+        qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
+        qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
+        qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
+    } else {
+        qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
+        qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
+        qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    }
 }
 
 struct Exact {
@@ -398,9 +421,8 @@ __device__ __forceinline__ void mandelbulb_p8_x2(uint32_t max_iters, float bailo
 // Polar form of src/shape/mandelbulb.frag:1-39 with a real power, evaluated
 // at q = R^T p.  GLSL length() is taken as sqrt((x*x + y*y) + z*z).
 __device__ __forceinline__ float polar_de(const ShapeDev& s, float px, float py, float pz) {
-    const float qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-    const float qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-    const float qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
+    float qx, qy, qz;
+    rotate_point(s, px, py, pz, qx, qy, qz);
     const float P = s.power_f;
     float zx = qx, zy = qy, zz = qz, dr = 1.0f, r = 0.0f;
     for (uint32_t i = 0; i < s.max_iters; ++i) {
@@ -612,9 +634,8 @@ __device__ __forceinline__ bool polar_step_fast(float P, float bailout, float qx
 }
 
 __device__ __forceinline__ float polar_de_fast(const ShapeDev& s, float px, float py, float pz) {
-    const float qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
-    const float qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
-    const float qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
+    float qx, qy, qz;
+    rotate_point<true>(s, px, py, pz, qx, qy, qz);
     float x = qx, y = qy, z = qz, dr = 1.0f, r = 0.0f;
     for (uint32_t i = 0; i < s.max_iters; ++i)
         if (!polar_step_fast(s.power_f, s.bailout, qx, qy, qz, x, y, z, dr, r)) break;

@@ -74,15 +74,7 @@ struct PolarIter {
     uint32_t it;
 
     __device__ __forceinline__ void start(const ShapeDev& s, float px, float py, float pz) {
-        if (FAST) {
-            qx = fmaf(s.m[0], px, fmaf(s.m[3], py, s.m[6] * pz));
-            qy = fmaf(s.m[1], px, fmaf(s.m[4], py, s.m[7] * pz));
-            qz = fmaf(s.m[2], px, fmaf(s.m[5], py, s.m[8] * pz));
-        } else {
-            qx = __fadd_rn(__fadd_rn(__fmul_rn(s.m[0], px), __fmul_rn(s.m[3], py)), __fmul_rn(s.m[6], pz));
-            qy = __fadd_rn(__fadd_rn(__fmul_rn(s.m[1], px), __fmul_rn(s.m[4], py)), __fmul_rn(s.m[7], pz));
-            qz = __fadd_rn(__fadd_rn(__fmul_rn(s.m[2], px), __fmul_rn(s.m[5], py)), __fmul_rn(s.m[8], pz));
-        }
+        rotate_point<FAST>(s, px, py, pz, qx, qy, qz);
         st = {qx, qy, qz, 1.0f};
         r = 0.0f;
         it = 0;

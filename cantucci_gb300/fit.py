@@ -131,5 +131,5 @@ def fit(target, cam, power0=8.0, rot0=(0.0, 0.0, 0.0), steps=300, lr=1e-2, max_s
         opt.step()
         losses.append(float(loss.detach()))
         if callback:
-            callback(it, float(power), rot.detach().tolist(), losses[-1])
-    return float(power), rot.detach().tolist(), losses
+            callback(it, float(power.detach()), rot.detach().tolist(), losses[-1])
+    return float(power.detach()), rot.detach().tolist(), losses

@@ -76,6 +76,36 @@ def lib():
     return _lib
 
 
+_ref_lib = None
+
+
+def ref_shader():
+    """The reference's own estimator shaders compiled as C++
+    (oracle/ref_build.py), or None where neither the reference tree nor an
+    earlier build is present."""
+    global _ref_lib
+    if _ref_lib is None:
+        from . import ref_build
+        path = ref_build.build()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        L.ref_shader_count.restype = C.c_int
+        L.ref_shader_de.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_void_p]
+        assert L.ref_shader_count() == len(ref_build.CONFIGS)
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_shader_de(config: int, points) -> np.ndarray:
+    """shape_de() of ref_build.CONFIGS[config] at each point (float32)."""
+    L = ref_shader()
+    pts = _f32(points).reshape(-1, 3)
+    out = np.empty(len(pts), np.float32)
+    L.ref_shader_de(config, pts.ctypes.data, len(pts), out.ctypes.data)
+    return out
+
+
 def default_threads() -> int:
     return max(1, os.cpu_count() or 1)
 

@@ -274,6 +274,14 @@ void orc_rotation_matrix(const float euler[3], float m[9]) {
     for (int i = 0; i < 9; i++) m[i] = (float)md[i];
 }
 
+/* Whether the polar form has a rotation.  Without one the point enters the
+ * estimator unchanged, as in src/shape/mandelbulb.frag (which has no
+ * rotation): a product with the identity would turn -0 into +0 and an
+ * infinite coordinate into NaN. */
+static inline int rotated(const orc_shape* s) {
+    return s->rot[0] != 0.0f || s->rot[1] != 0.0f || s->rot[2] != 0.0f;
+}
+
 /* q = R^T p in f32, sums left to right. */
 static inline void rot_apply_t(const float m[9], float px, float py, float pz,
                                float* qx, float* qy, float* qz) {
@@ -286,8 +294,8 @@ static inline void rot_apply_t(const float m[9], float px, float py, float pz,
  * GLSL length() is taken as sqrt((x*x + y*y) + z*z). */
 static float polar_de_f32(const orc_shape* s, const float m[9], float px, float py, float pz,
                           uint32_t* steps_out) {
-    float qx, qy, qz;
-    rot_apply_t(m, px, py, pz, &qx, &qy, &qz);
+    float qx = px, qy = py, qz = pz;
+    if (rotated(s)) rot_apply_t(m, px, py, pz, &qx, &qy, &qz);
     const float P = s->power_f;
     float zx = qx, zy = qy, zz = qz, dr = 1.0f, r = 0.0f;
     uint32_t steps = 0;
@@ -479,9 +487,12 @@ static double mb_de_int_d(uint32_t P, uint64_t max_iters, double bailout,
 
 static double polar_de_d(const orc_shape* s, const double m[9], double px, double py, double pz,
                          uint32_t* steps_out) {
-    double qx = m[0] * px + m[3] * py + m[6] * pz;
-    double qy = m[1] * px + m[4] * py + m[7] * pz;
-    double qz = m[2] * px + m[5] * py + m[8] * pz;
+    double qx = px, qy = py, qz = pz;
+    if (rotated(s)) {
+        qx = m[0] * px + m[3] * py + m[6] * pz;
+        qy = m[1] * px + m[4] * py + m[7] * pz;
+        qz = m[2] * px + m[5] * py + m[8] * pz;
+    }
     const double P = s->power_f;
     double zx = qx, zy = qy, zz = qz, dr = 1.0, r = 0.0;
     uint32_t steps = 0;
@@ -690,9 +701,12 @@ static void de_grad_f64_m(const orc_shape* s, const double m[9], double px, doub
         out[4] = d.d[3];
         return;
     }
-    double qx = m[0] * px + m[3] * py + m[6] * pz;
-    double qy = m[1] * px + m[4] * py + m[7] * pz;
-    double qz = m[2] * px + m[5] * py + m[8] * pz;
+    double qx = px, qy = py, qz = pz;
+    if (rotated(s)) {
+        qx = m[0] * px + m[3] * py + m[6] * pz;
+        qy = m[1] * px + m[4] * py + m[7] * pz;
+        qz = m[2] * px + m[5] * py + m[8] * pz;
+    }
     double P = s->kind == ORC_MANDELBULB_POLAR ? (double)s->power_f : (double)s->power;
     dual d = polar_de_dual(qx, qy, qz, P, s->max_iters, s->bailout);
     out[0] = d.v;

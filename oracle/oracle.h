@@ -8,12 +8,18 @@
  * links, loads or calls it.
  *
  * Parity status: the reference (Rust, nightly, x86-64 SSE4.1 only) has no
- * unit tests and no golden vectors, and cannot be built on this machine.
- * Every formula below follows the cited reference line in operation order
- * and rounding (f32, no contraction, glibc libm where Rust std calls libm),
- * but the pin against the reference's own outputs is absent: parity is
- * unpinned by the reference; golden fixtures are generated from this oracle
- * on x86-64 (the reference's only platform) by tests/golden/make_golden.py.
+ * unit tests and no golden vectors, and its Rust code cannot be built on
+ * this machine.  Every formula below follows the cited reference line in
+ * operation order and rounding (f32, no contraction, glibc libm where Rust
+ * std calls libm).
+ *   - The polar and sphere estimators are pinned: they give the same bits
+ *     as the reference's own shader source (src/shape/mandelbulb.frag,
+ *     src/shape/shape.frag) compiled as C++ by oracle/ref_build.py
+ *     (fixture tests/golden/shader_de.npz).
+ *   - The P=8 polynomial, the generic-trig path and the mesher are
+ *     unpinned by the reference; their golden fixtures are generated from
+ *     this oracle on x86-64 (the reference's only platform) by
+ *     tests/golden/make_golden.py.
  */
 #ifndef CANTUCCI_ORACLE_H
 #define CANTUCCI_ORACLE_H

@@ -202,6 +202,35 @@ def test_sphere_bit_exact(cg, orc):
     assert np.array_equal(d.view(np.uint32), ref.view(np.uint32))
 
 
+def test_reference_shaders_fixture(cg):
+    """The GPU's sphere and polar estimators against cantucci's own shaders
+    (src/shape/shape.frag, src/shape/mandelbulb.frag) compiled as C++ with
+    their placeholders filled as the shapes fill them, at 5371 points
+    including signed zeros, infinities and NaN coordinates
+    (tests/golden/shader_de.npz, made by tests/golden/make_shader_golden.py).
+    Sphere: the same bits (IEEE operations only).  Polar form at P = 3, 6,
+    8, 10: CUDA's acosf/atan2f/powf/sincosf/logf against glibc's, so the
+    bar of test_polar_vs_oracle (>= 99.9% same sign, >= 99% within
+    1e-5 + 1e-4 |d|), and NaN where the shader gives NaN."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "shader_de.npz"))
+    pts = g["points"]
+    for name, kind, par in zip(g["names"], g["kinds"], g["params"]):
+        ref = g["de_" + str(name)]
+        nan = np.isnan(ref)
+        if str(kind) == "sphere":
+            d = cg.Sphere(tuple(float(v) for v in par[:3]), float(par[3])).batch_min_distance_from(pts)
+            assert np.array_equal(np.isnan(d), nan), name
+            assert np.array_equal(d[~nan].view(np.uint32), ref[~nan].view(np.uint32)), name
+            continue
+        d = cg.MandelbulbPolar(float(par[0]), int(par[1]), float(par[2])).batch_min_distance_from(pts)
+        assert np.mean(np.isnan(d) == nan) >= 0.999, name
+        fin = np.isfinite(ref) & np.isfinite(d)
+        assert np.mean(np.signbit(d[fin]) == np.signbit(ref[fin])) >= 0.999, name
+        assert np.mean(np.abs(d[fin] - ref[fin]) <= 1e-5 + 1e-4 * np.abs(ref[fin])) >= 0.99, name
+
+
 def test_march_matches_golden(cg, golden):
     hits, hit = cg.march(cg.Mandelbulb(8, 15, 2.5), golden["march_origins"], golden["march_dirs"],
                          100, 1e-6)

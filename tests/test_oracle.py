@@ -6,6 +6,7 @@ that pass through libm are compared to a few ulp and everything computed
 with IEEE add/mul/div/sqrt only is still compared bit for bit.
 """
 import hashlib
+import os
 import platform
 
 import numpy as np
@@ -216,3 +217,63 @@ def test_qef_model(orc):
     dq = np.abs(orc.de_f64(mb, v.astype(np.float32)))
     dc = np.abs(orc.de_f64(mb, m["vertices"]["position"]))
     assert np.median(dq) < 0.5 * np.median(dc)
+
+
+# ---- the reference's own estimator shaders (oracle/ref_build.py) --------
+
+SHADER_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "shader_de.npz")
+
+
+def shader_shape(orc, kind, par):
+    """The oracle shape a filled shader describes: mandelbulb.frag with
+    power P is the polar form at power P without rotation."""
+    if kind == "mandelbulb":
+        return orc.mandelbulb_polar(float(par[0]), int(par[1]), float(par[2]), (0.0, 0.0, 0.0))
+    return orc.sphere(tuple(float(v) for v in par[:3]), float(par[3]))
+
+
+def shader_agrees(ours, ref):
+    """Same bits wherever the shader's value is a number (on x86-64; 2 ulps
+    elsewhere, where libm differs), NaN on both sides where it is NaN (the
+    oracle returns x86's default NaN for every NaN; the compiled shader keeps
+    the sign glibc gives)."""
+    ours = np.asarray(ours, np.float32)
+    ref = np.asarray(ref, np.float32)
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(ours), nan)
+    return same_bits_or_close(ours[~nan], ref[~nan], 2)
+
+
+def test_oracle_matches_reference_shader_fixture(orc):
+    """The oracle's polar and sphere estimators against cantucci's own
+    shaders (src/shape/mandelbulb.frag, src/shape/shape.frag) compiled as
+    C++ with their placeholders filled as src/shape/mandelbulb.rs:82-85 and
+    src/shape/sphere.rs:42-46 fill them (tests/golden/make_shader_golden.py):
+    five Mandelbulb powers and two spheres at 5371 points, including signed
+    zeros, infinities and NaN coordinates."""
+    g = np.load(SHADER_GOLDEN)
+    pts = g["points"]
+    assert np.array_equal(pts[:20], W.bench_points())
+    for name, kind, par in zip(g["names"], g["kinds"], g["params"]):
+        ours = orc.min_distance_from(shader_shape(orc, str(kind), par), pts)
+        assert shader_agrees(ours, g["de_" + str(name)]), name
+
+
+def test_oracle_matches_reference_shader_live(orc):
+    """The same against the shader library built from the reference tree
+    here, at 200,000 further seeded points (skipped where the reference tree
+    and an earlier build are both absent)."""
+    if orc.ref_shader() is None:
+        pytest.skip("reference shaders not built")
+    from oracle import ref_build
+    g = np.load(SHADER_GOLDEN)
+    rng = np.random.default_rng(77)
+    pts = rng.uniform(-1.6, 1.6, (200_000, 3)).astype(np.float32)
+    for i, (name, kind, par) in enumerate(ref_build.CONFIGS):
+        ref = orc.ref_shader_de(i, pts)
+        assert shader_agrees(orc.min_distance_from(shader_shape(orc, kind, par), pts), ref), name
+        # the fixture is what this build computes
+        fx = orc.ref_shader_de(i, g["points"])
+        assert np.array_equal(np.isnan(fx), np.isnan(g["de_" + name]))
+        ok = ~np.isnan(fx)
+        assert np.array_equal(fx[ok].view(np.uint32), g["de_" + name][ok].view(np.uint32)), name
