@@ -897,7 +897,10 @@ def run_ours(args, rank, world, local_rank):
     e2e = {"value": world * n_pts * args.steps / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": C.sizeof(_ffi.CgSpan) + C.sizeof(_ffi.CgShape),
            "d2h_bytes_per_step": nv * 28 + ni * 4 + 16,
-           "note": "inputs are the span and shape (kernel parameters); outputs are the mesh"}
+           "gpu_launches_per_step": LAUNCHES_PER_MESH + 1,
+           "note": "inputs are the span and shape (kernel parameters); outputs are the mesh, "
+                   "the vertices stored by k_place into the pinned buffer, the indices copied "
+                   "there by k_copy_words beside it"}
 
     # Roofline of the dominant kernel (k_de_grid): algorithmic flops from the
     # rotate steps actually executed, over its CUDA-event time per launch.
