@@ -115,16 +115,24 @@ __global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float*
 }
 
 // params[k] += the sum over warps w < nwarps of partial[4 w + k], in a fixed
-// order (one block: strided sequential sums, then a fixed tree).
+// order (one block: strided sequential sums of one 16-byte load per warp,
+// then a fixed tree).  `partial` is 16-byte aligned.
 __global__ void __launch_bounds__(256) k_sum_partials4(const float* __restrict__ partial,
                                                        uint32_t nwarps, float* __restrict__ params) {
     __shared__ float sh[4][256];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        float v = 0.0f;
-        for (uint32_t w = threadIdx.x; w < nwarps; w += 256) v += partial[4 * w + k];
-        sh[k][threadIdx.x] = v;
+    const float4* p4 = reinterpret_cast<const float4*>(partial);
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (uint32_t w = threadIdx.x; w < nwarps; w += 256) {
+        const float4 q = p4[w];
+        v.x += q.x;
+        v.y += q.y;
+        v.z += q.z;
+        v.w += q.w;
     }
+    sh[0][threadIdx.x] = v.x;
+    sh[1][threadIdx.x] = v.y;
+    sh[2][threadIdx.x] = v.z;
+    sh[3][threadIdx.x] = v.w;
     __syncthreads();
     for (uint32_t half = 128; half > 0; half >>= 1) {
         if (threadIdx.x < half)
@@ -133,6 +141,69 @@ __global__ void __launch_bounds__(256) k_sum_partials4(const float* __restrict__
         __syncthreads();
     }
     if (threadIdx.x < 4) params[threadIdx.x] += sh[threadIdx.x][0];
+}
+
+// The calling thread's partials buffer on the current device, grown as
+// needed and reused across calls.  A call waits on `st` (not on the host)
+// for the previous call's use of the buffer, whatever its stream, and
+// release_partials() marks the end of its own use.  While `st` is being
+// captured into a graph, a stream-ordered allocation takes its place (it
+// becomes a node of the graph; an event from outside the capture could
+// not be waited on).
+namespace {
+struct PartialBuf {
+    int device = -1;
+    float* p = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    ~PartialBuf() {
+        if (p) cudaFree(p);  // errors at process exit are of no consequence
+        if (done) cudaEventDestroy(done);
+    }
+};
+thread_local PartialBuf t_partials[16];
+}  // namespace
+
+static bool capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+cg_status acquire_partials(size_t floats, cudaStream_t st, float** out) {
+    if (capturing(st)) {
+        CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(out), floats * sizeof(float), st));
+        return CG_OK;
+    }
+    int dev = 0;
+    CG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 16) {
+        set_error("device ordinal %d out of range", dev);
+        return CG_EINVAL;
+    }
+    PartialBuf& b = t_partials[dev];
+    if (!b.done) CG_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
+    else CG_CUDA(cudaStreamWaitEvent(st, b.done, 0));
+    if (b.cap < floats) {
+        CG_CUDA(cudaEventSynchronize(b.done));  // the old buffer is idle before it goes
+        if (b.p) CG_CUDA(cudaFree(b.p));
+        b.p = nullptr;
+        b.cap = 0;
+        CG_CUDA(cudaMalloc(&b.p, floats * sizeof(float)));
+        b.cap = floats;
+    }
+    *out = b.p;
+    return CG_OK;
+}
+
+cg_status release_partials(float* partial, cudaStream_t st) {
+    if (capturing(st)) {
+        CG_CUDA(cudaFreeAsync(partial, st));
+        return CG_OK;
+    }
+    int dev = 0;
+    CG_CUDA(cudaGetDevice(&dev));
+    CG_CUDA(cudaEventRecord(t_partials[dev].done, st));
+    return CG_OK;
 }
 
 cg_status launch_sum_partials4(const float* partial, uint32_t nwarps, float* params,
@@ -283,12 +354,15 @@ cg_status cg_de_backward(const cg_shape* shape, const float* points, const float
     const unsigned G = grid_for(n, 128, 16);
     const uint32_t nwarps = G * 4;
     float* partial = nullptr;
-    if (grad_params) CG_CUDA(cudaMallocAsync(&partial, (size_t)nwarps * 4 * sizeof(float), st));
+    if (grad_params) CG_TRY(acquire_partials((size_t)nwarps * 4, st, &partial));
     k_de_vjp<<<G, 128, 0, st>>>(make_shape_dev(*shape), rotation_derivatives(*shape), points,
                                 grad_out, n, grad_points, partial);
     cg_status rs = cuda_status(cudaGetLastError(), "k_de_vjp", __FILE__, __LINE__);
     if (rs == CG_OK && partial) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
-    if (partial) cudaFreeAsync(partial, st);
+    if (partial) {
+        const cg_status rr = release_partials(partial, st);
+        if (rs == CG_OK) rs = rr;
+    }
     return rs;
 }
 

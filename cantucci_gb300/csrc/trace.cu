@@ -334,12 +334,12 @@ cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, cons
     const unsigned G = grid_for(n, 128, 16);
     const uint32_t nwarps = G * 4;
     float* partial = nullptr;
-    CG_CUDA(cudaMallocAsync(&partial, (size_t)nwarps * 4 * sizeof(float), st));
+    CG_TRY(acquire_partials((size_t)nwarps * 4, st, &partial));
     k_trace_backward<<<G, 128, 0, st>>>(s, c, dm, depth, grad_depth, partial);
     cg_status rs = cuda_status(cudaGetLastError(), "k_trace_backward", __FILE__, __LINE__);
     if (rs == CG_OK) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
-    cudaFreeAsync(partial, st);
-    return rs;
+    const cg_status rr = release_partials(partial, st);
+    return rs == CG_OK ? rr : rs;
 }
 
 }  // extern "C"

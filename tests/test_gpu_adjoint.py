@@ -134,6 +134,52 @@ def test_autograd_function(cg):
                                rtol=1e-3, atol=1e-4)
 
 
+def test_backward_partials_reuse_and_capture(cg):
+    """The parameter gradients' per-warp partials live in a buffer of the
+    calling thread that later calls reuse: calls alternating between two
+    streams, a larger call that grows the buffer, and a call captured in a
+    CUDA graph (which allocates its own) all give the first call's bits."""
+    import ctypes as C
+    import torch
+    from cantucci_gb300 import _ffi
+    lib = cg.load()
+    shape = cg.MandelbulbPolar(8.3, 15, 2.5, (0.2, 0.1, 0.0))._cshape()
+
+    def backward(pts, g, params, stream):
+        _ffi.check(lib.cg_de_backward(C.byref(shape), C.c_void_p(pts.data_ptr()),
+                                      C.c_void_p(g.data_ptr()), pts.shape[0], None,
+                                      C.c_void_p(params.data_ptr()),
+                                      C.c_void_p(stream.cuda_stream)))
+
+    small = band_points(cg, 4096, 8.3, (0.2, 0.1, 0.0), seed=5)
+    large = band_points(cg, 1 << 19, 8.3, (0.2, 0.1, 0.0), seed=6)
+    gs = torch.linspace(-1, 1, small.shape[0], device="cuda")
+    gl = torch.linspace(-1, 1, large.shape[0], device="cuda")
+    s0, s1 = torch.cuda.Stream(), torch.cuda.Stream()
+    want_s, want_l = torch.empty(4, device="cuda"), torch.empty(4, device="cuda")
+    backward(small, gs, want_s, s0)
+    s0.synchronize()
+    backward(large, gl, want_l, s0)
+    s0.synchronize()
+    outs = [torch.empty(4, device="cuda") for _ in range(6)]
+    for k, o in enumerate(outs):
+        st = s0 if k % 2 == 0 else s1
+        backward(large if k == 3 else small, gl if k == 3 else gs, o, st)
+    torch.cuda.synchronize()
+    for k, o in enumerate(outs):
+        want = want_l if k == 3 else want_s
+        assert torch.equal(o.view(torch.int32), want.view(torch.int32)), k
+    # captured: the graph replays the same sums
+    gout = torch.empty(4, device="cuda")
+    cap = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=cap):
+        backward(small, gs, gout, cap)
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(gout.view(torch.int32), want_s.view(torch.int32))
+
+
 def test_fd_grad_matches_adjoint_on_smooth_points(cg):
     """GPU six-evaluation central differences agree with the adjoint where
     the field is smooth at the step."""
