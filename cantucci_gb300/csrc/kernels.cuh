@@ -169,9 +169,9 @@ size_t scan_scratch_words(uint32_t n);
 // fixed order (deterministic parameter gradients).
 cg_status launch_sum_partials4(const float* partial, uint32_t nwarps, float* params,
                                cudaStream_t st);
-// The calling thread's per-warp partials buffer (at least `floats` floats,
-// 16-byte aligned) for work enqueued on `st`; release_partials(p, st) after
-// the last launch that uses it.
+// The calling thread's scratch buffer (at least `floats` words, 16-byte
+// aligned: per-warp partial sums, a work-queue counter) for work enqueued
+// on `st`; release_partials(p, st) after the last launch that uses it.
 cg_status acquire_partials(size_t floats, cudaStream_t st, float** out);
 cg_status release_partials(float* partial, cudaStream_t st);
 

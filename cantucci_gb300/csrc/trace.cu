@@ -293,8 +293,10 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
         CG_CHECK_LAUNCH("k_trace");
         return CG_OK;
     }
-    uint32_t* next = nullptr;
-    CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&next), sizeof(uint32_t), st));
+    // the work queue's counter: the first word of the thread's scratch buffer
+    float* scratch = nullptr;
+    CG_TRY(acquire_partials(4, st, &scratch));
+    uint32_t* next = reinterpret_cast<uint32_t*>(scratch);
     CG_CUDA(cudaMemsetAsync(next, 0, sizeof(uint32_t), st));
     switch (mode_of(s, numerics)) {
     case MODE_P8: launch_trace_queue<MODE_P8>(s, c, max_steps, eps_scale, depth, next, st); break;
@@ -312,7 +314,7 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     default: launch_trace_queue<MODE_SPHERE>(s, c, max_steps, eps_scale, depth, next, st); break;
     }
     const cudaError_t le = cudaGetLastError();
-    CG_CUDA(cudaFreeAsync(next, st));
+    CG_TRY(release_partials(scratch, st));
     CG_CUDA(le);
     return CG_OK;
 }
