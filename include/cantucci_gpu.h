@@ -448,7 +448,12 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
  * x = eye + t d, DE(x; theta) = 0 gives dt/dtheta = -(dDE/dtheta) /
  * (grad_x DE . d).  Sums grad_depth[i] * dt_i/d(power, a, b, c) over hit
  * pixels into grad_params (device, 4 floats; per-warp partial sums added in
- * a fixed order, so the result is reproducible).  No reference counterpart. */
+ * a fixed order, so the result is reproducible).  No reference counterpart.
+ * The partial sums (and cg_trace_depth's work-queue counter) live in a
+ * scratch buffer of the calling host thread: a call's GPU work waits for
+ * the previous call's use of it, on whichever stream that ran.  While
+ * `stream` is being captured into a CUDA graph, the call allocates its own
+ * (a stream-ordered allocation, captured as a graph node). */
 cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, const float* depth,
                             const float* grad_depth, float* grad_params, void* stream);
 
@@ -488,7 +493,8 @@ cg_status cg_de_spatial_grad(const cg_shape* shape, const float* points, uint64_
  * upstream gradient g (device, n floats), writes g[i] * dDE/dp_i to
  * grad_points (device n x 3, may be NULL) and the sums over i of
  * g[i] * dDE/d(power, a, b, c) to grad_params (device, 4 floats, may be NULL;
- * summed in a fixed order, so the result is reproducible). */
+ * summed in a fixed order, so the result is reproducible).  Its partial sums
+ * use the calling thread's scratch buffer, as cg_trace_backward's do. */
 cg_status cg_de_backward(const cg_shape* shape, const float* points, const float* grad_out,
                          uint64_t n, float* grad_points, float* grad_params, void* stream);
 
