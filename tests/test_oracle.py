@@ -277,3 +277,14 @@ def test_oracle_matches_reference_shader_live(orc):
         assert np.array_equal(np.isnan(fx), np.isnan(g["de_" + name]))
         ok = ~np.isnan(fx)
         assert np.array_equal(fx[ok].view(np.uint32), g["de_" + name][ok].view(np.uint32)), name
+
+
+def test_shader_placeholder_formatting():
+    """The recipe fills the shaders' placeholders with Rust's Display of an
+    f32 (shortest round-trip digits, no exponent, no trailing ".0"), as
+    src/shape/mandelbulb.rs:83 and src/shape/sphere.rs:43-46 do."""
+    from oracle.ref_build import rust_f32
+    cases = {2.5: "2.5", 5.0: "5", -0.05: "-0.05", 1e-7: "0.0000001", 1e10: "10000000000",
+             0.1: "0.1", -0.0: "-0", 8.3: "8.3", 1.0 / 3.0: "0.33333334"}
+    for v, want in cases.items():
+        assert rust_f32(v) == want, (v, rust_f32(v))
