@@ -106,6 +106,106 @@ def ref_shader_de(config: int, points) -> np.ndarray:
     return out
 
 
+class RustRefShape(C.Structure):
+    """rustref_shape of oracle/rust_build.py's C entry points."""
+    _fields_ = [("kind", C.c_int32), ("power", C.c_int32), ("max_iters", C.c_uint64),
+                ("bailout", C.c_float), ("center", C.c_float * 3), ("radius", C.c_float)]
+
+
+RR_OK, RR_ASSERT, RR_CAPACITY, RR_LERP, RR_INDEX, RR_EINVAL = 0, 1, 2, 3, 4, 5
+_rust_lib = None
+
+
+def rust_ref():
+    """The reference's own Rust source for the estimator and the mesher,
+    translated into C++ by oracle/rust_build.py, or None where neither the
+    reference tree nor an earlier build is present."""
+    global _rust_lib
+    if _rust_lib is None:
+        from . import rust_build
+        try:
+            path = rust_build.build()
+        except Exception:  # no compiler for the x86-only source (e.g. an Arm host)
+            path = rust_build.LIB if os.path.exists(rust_build.LIB) else None
+        if path is None:
+            return None
+        try:
+            L = C.CDLL(path)
+        except OSError:  # built on another architecture
+            return None
+        sp = C.POINTER(RustRefShape)
+        L.rustref_de.argtypes = [sp, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.rustref_contains.argtypes = [sp, C.c_void_p, C.c_uint64, C.c_void_p]
+        L.rustref_generate_for_box.argtypes = [sp, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64,
+                                               C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64),
+                                               C.POINTER(C.c_uint64), C.c_void_p, C.c_void_p]
+        _rust_lib = L
+    return _rust_lib
+
+
+def _rust_shape(shape: Shape) -> RustRefShape:
+    r = RustRefShape()
+    if shape.kind == ORC_SPHERE:
+        r.kind = 1
+        for i in range(3):
+            r.center[i] = shape.center[i]
+        r.radius = shape.radius
+    elif shape.kind == ORC_MANDELBULB:
+        r.kind = 0
+        r.power = shape.power
+        r.max_iters = shape.max_iters
+        r.bailout = shape.bailout
+    else:
+        raise ValueError("the reference's Rust source has integer-power Mandelbulbs and Spheres")
+    return r
+
+
+def rust_ref_de(shape: Shape, points) -> np.ndarray:
+    """Shape::min_distance_from of the translated reference at each point."""
+    pts = _f32(points).reshape(-1, 3)
+    out = np.empty(len(pts), np.float32)
+    rc = rust_ref().rustref_de(C.byref(_rust_shape(shape)), pts.ctypes.data, len(pts),
+                               out.ctypes.data)
+    if rc != RR_OK:
+        raise RuntimeError("rustref_de failed with %d" % rc)
+    return out
+
+
+def rust_ref_contains(shape: Shape, points) -> np.ndarray:
+    pts = _f32(points).reshape(-1, 3)
+    out = np.empty(len(pts), np.uint8)
+    rc = rust_ref().rustref_contains(C.byref(_rust_shape(shape)), pts.ctypes.data, len(pts),
+                                     out.ctypes.data)
+    if rc != RR_OK:
+        raise RuntimeError("rustref_contains failed with %d" % rc)
+    return out.astype(bool)
+
+
+def rust_ref_generate_for_box(shape: Shape, span, res: int, vcap=None, icap=None):
+    """MeshBuffer::generate_for_box of the translated reference.  Returns
+    dict(rc, nv, ni, vertices, indices, dists, points); rc RR_LERP means the
+    reference panics in lerp (dists and points are still filled)."""
+    sp = _f32(span).reshape(6)
+    N = res + 1
+    vcap = res ** 3 if vcap is None else vcap
+    icap = 18 * res ** 3 if icap is None else icap
+    verts = np.empty(vcap, VERTEX_DTYPE)
+    idx = np.empty(icap, np.uint32)
+    dists = np.full(N ** 3, np.nan, np.float32)
+    points = np.zeros(res ** 3, np.uint32)
+    nv, ni = C.c_uint64(), C.c_uint64()
+    rc = rust_ref().rustref_generate_for_box(C.byref(_rust_shape(shape)), sp.ctypes.data, res,
+                                             verts.ctypes.data, vcap, idx.ctypes.data, icap,
+                                             C.byref(nv), C.byref(ni), dists.ctypes.data,
+                                             points.ctypes.data)
+    out = dict(rc=rc, nv=nv.value, ni=ni.value, dists=dists.reshape(N, N, N),
+               points=points.reshape(res, res, res))
+    if rc == RR_OK:
+        out["vertices"] = verts[:nv.value].copy()
+        out["indices"] = idx[:ni.value].copy()
+    return out
+
+
 def default_threads() -> int:
     return max(1, os.cpu_count() or 1)
 

@@ -9,8 +9,8 @@
  * Contraction must stay off: Rust never fuses a*b+c, so every product and sum
  * below is rounded to f32 on its own, in the order the reference writes it.
  *
- * Parity: unpinned by the reference (it ships no tests or golden vectors and
- * cannot be built here); see oracle.h.
+ * Parity: pinned bit for bit to the reference's own Rust source, translated
+ * into C++ by oracle/rust_build.py; see oracle.h.
  */
 #define _GNU_SOURCE
 #include "oracle.h"

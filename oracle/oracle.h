@@ -7,19 +7,24 @@
  * baseline leg, and by nothing else.  The product (cantucci_gb300/) never
  * links, loads or calls it.
  *
- * Parity status: the reference (Rust, nightly, x86-64 SSE4.1 only) has no
- * unit tests and no golden vectors, and its Rust code cannot be built on
- * this machine.  Every formula below follows the cited reference line in
+ * Parity status: pinned to the reference's own source.  The reference
+ * (Rust, nightly, x86-64 SSE4.1 only) has no unit tests and no golden
+ * vectors, and no Rust toolchain exists here, so its source text is compiled
+ * another way.  Every formula below follows the cited reference line in
  * operation order and rounding (f32, no contraction, glibc libm where Rust
- * std calls libm).
- *   - The polar and sphere estimators are pinned: they give the same bits
- *     as the reference's own shader source (src/shape/mandelbulb.frag,
- *     src/shape/shape.frag) compiled as C++ by oracle/ref_build.py
- *     (fixture tests/golden/shader_de.npz).
- *   - The P=8 polynomial, the generic-trig path and the mesher are
- *     unpinned by the reference; their golden fixtures are generated from
- *     this oracle on x86-64 (the reference's only platform) by
- *     tests/golden/make_golden.py.
+ * std calls libm), and:
+ *   - the integer-power estimator (the P=8 polynomial, the generic-trig and
+ *     z-axis paths), the sphere and the whole mesher give the same bits as
+ *     the reference's Rust source translated mechanically into C++ by
+ *     oracle/rust_build.py (fixture tests/golden/rust_ref.npz); at a point
+ *     with a NaN coordinate only NaN-ness is defined (the NaN an SSE
+ *     operation with two NaN operands returns depends on the operand order
+ *     the compiler picks);
+ *   - the polar and sphere estimators give the same bits as the reference's
+ *     own shader source (src/shape/mandelbulb.frag, src/shape/shape.frag)
+ *     compiled as C++ by oracle/ref_build.py (tests/golden/shader_de.npz).
+ * tests/golden/golden.npz (tests/golden/make_golden.py) holds this oracle's
+ * outputs on x86-64; tests/test_rust_pin.py checks it against the pin.
  */
 #ifndef CANTUCCI_ORACLE_H
 #define CANTUCCI_ORACLE_H

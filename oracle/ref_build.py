@@ -9,7 +9,8 @@ The shape fills the placeholders with Rust's Display of its parameters
 power and iteration count as integers, f32 values as their shortest
 round-trip decimal without an exponent ("2.5", "5", "-0.05").
 
-This recipe reads those two files where they lie in the reference tree,
+This recipe reads those two files where they lie in the reference tree (the
+directory named by the CANTUCCI_REFERENCE environment variable),
 fills them the same way for each entry of CONFIGS, and writes the filled
 text only under oracle/_ref/ (git-ignored), together with a generated
 wrapper that puts each filled shader in its own namespace over the GLSL
@@ -31,7 +32,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libref_shader.so")
-REFERENCE = os.environ.get("CANTUCCI_REFERENCE", "/root/reference")
+# The cantucci source tree; the recipe does nothing without it.
+REFERENCE = os.environ.get("CANTUCCI_REFERENCE")
 SHADERS = {"mandelbulb": "src/shape/mandelbulb.frag", "sphere": "src/shape/shape.frag"}
 
 # (name, kind, parameters).  Mandelbulb: power (integer), max_iters, bailout.
@@ -76,7 +78,8 @@ def fill(kind: str, params) -> str:
 
 
 def available() -> bool:
-    return all(os.path.exists(os.path.join(REFERENCE, p)) for p in SHADERS.values())
+    return bool(REFERENCE) and all(os.path.exists(os.path.join(REFERENCE, p))
+                                   for p in SHADERS.values())
 
 
 def _wrapper() -> str:

@@ -1,0 +1,118 @@
+"""The GPU path against cantucci's own Rust source, through the fixture
+tests/golden/rust_ref.npz (the reference's estimator and mesher translated
+into C++ by oracle/rust_build.py; the GPU machine has no reference tree).
+
+Bar:
+  - Mandelbulb<8>: every distance's sign bit for bit (NaNs the estimator
+    makes carry x86's 0xFFC00000), values within 2 ulp (CUDA's logf against
+    glibc's in the final ln r); the cell table and index list of every mesh
+    bit for bit, and the sign of every corner distance;
+  - Sphere (no libm): distances and whole meshes, vertices included, bit for
+    bit;
+  - integer powers through acosf/atan2f/sinf/cosf: CUDA's and glibc's differ
+    in the last bit, so 99% within 1e-3 relative and sign flips only where
+    the reference's own |DE| is below 1e-4.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rust_ref.npz")
+DE_ULPS = 2
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def ulp_diff(a, b):
+    a = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    a = np.where(a < 0, -(a & 0x7FFFFFFF), a)
+    b = np.where(b < 0, -(b & 0x7FFFFFFF), b)
+    return np.abs(a - b)
+
+
+@pytest.fixture(scope="module")
+def rg():
+    return np.load(FIXTURE)
+
+
+@pytest.fixture(scope="module")
+def mesher(cg):
+    m = cg.Mesher(0)
+    yield m
+    m.close()
+
+
+def points_and_ref(rg, name):
+    """Bench, edge (without NaN coordinates: Rust leaves the NaN an operation
+    on a NaN operand returns unspecified) and seeded points, with the
+    translated reference's distances there."""
+    edge = rg["edge_points"]
+    keep = ~np.isnan(edge).any(axis=1)
+    pts = np.concatenate([rg["bench_points"], edge[keep], rg["rand_head"]])
+    ref = np.concatenate([rg["de_bench_" + name], rg["de_edge_" + name][keep],
+                          rg["de_rand_head_" + name]])
+    return pts, ref
+
+
+def test_p8_distances_vs_reference_source(cg, rg):
+    for name, (p, it, b) in zip(rg["de_names"], rg["de_configs"]):
+        name = str(name)
+        if int(p) != 8:
+            continue
+        pts, ref = points_and_ref(rg, name)
+        d = cg.Mandelbulb(int(p), int(it), float(b)).batch_min_distance_from(pts)
+        nan = np.isnan(ref)
+        assert np.array_equal(np.isnan(d), nan), name
+        assert np.all(d[nan].view(np.uint32) == ref[nan].view(np.uint32)), name
+        assert np.array_equal(np.signbit(d), np.signbit(ref)), name
+        assert ulp_diff(d[~nan], ref[~nan]).max() <= DE_ULPS, name
+
+
+def test_trig_powers_vs_reference_source(cg, rg):
+    for name, (p, it, b) in zip(rg["de_names"], rg["de_configs"]):
+        name = str(name)
+        if int(p) == 8:
+            continue
+        pts, ref = points_and_ref(rg, name)
+        d = cg.Mandelbulb(int(p), int(it), float(b)).batch_min_distance_from(pts)
+        fin = np.isfinite(ref) & np.isfinite(d)
+        close = np.abs(d[fin] - ref[fin]) <= 1e-6 + 1e-3 * np.abs(ref[fin])
+        assert close.mean() >= 0.99, (name, close.mean())
+        flip = fin & (np.signbit(d) != np.signbit(ref))
+        assert np.all(np.abs(ref[flip]) < 1e-4), (name, np.abs(ref[flip]).max())
+
+
+def test_sphere_distances_vs_reference_source(cg, rg):
+    edge = rg["edge_points"]
+    keep = ~np.isnan(edge).any(axis=1)
+    d = cg.Sphere((0.1, -0.05, 0.02), 0.9).batch_min_distance_from(edge[keep])
+    assert np.array_equal(d.view(np.uint32), rg["de_edge_sphere"][keep].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["c1", "p8_r16", "p8_r8_leaf", "sphere_r16"])
+def test_meshes_vs_reference_source(cg, rg, mesher, name):
+    """The cell table, the index list and the corner signs of each fixture
+    mesh bit for bit; the sphere's whole mesh bit for bit."""
+    span = rg["mesh_%s_span" % name]
+    res = int(rg["mesh_%s_res" % name])
+    shape = (cg.Sphere((0.1, -0.05, 0.02), 0.9) if name.startswith("sphere")
+             else cg.Mandelbulb(8, 15, 2.5))
+    buf, _ = cg.MeshBuffer.generate_for_box(cg.Span(span[:3], span[3:]), shape, res,
+                                            mesher=mesher)
+    assert [len(buf.vertices), len(buf.indices)] == rg["mesh_%s_counts" % name].tolist()
+    assert sha(buf.indices) == str(rg["mesh_%s_sha_indices" % name])
+    pts = mesher.last_points().cpu().numpy().astype(np.uint32)
+    assert sha(pts) == str(rg["mesh_%s_sha_points" % name])
+    d = mesher.last_dists().cpu().numpy()
+    assert sha(np.packbits(np.signbit(d))) == str(rg["mesh_%s_signbits_sha" % name])
+    if name.startswith("sphere"):
+        assert sha(d) == str(rg["mesh_%s_sha_dists" % name])
+        v = np.ascontiguousarray(buf.vertices)
+        assert sha(v) == str(rg["mesh_%s_sha_vertices" % name])
