@@ -138,6 +138,7 @@ SIGNATURES = [
     ("cg_march", _i32, [_shp, _vp, _vp, _u64, _u32, _f32, _vp, _vp, _vp]),
     ("cg_trace_depth", _i32, [_shp, C.c_void_p, _u32, _f32, _u32, _vp, _vp]),
     ("cg_trace_backward", _i32, [_shp, C.c_void_p, _vp, _vp, _vp, _vp]),
+    ("cg_trace_backward_capped", _i32, [_shp, C.c_void_p, _vp, _vp, _f32, _vp, _vp]),
     ("cg_de_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),
     ("cg_de_grad_tangent", _i32, [_shp, _vp, _u64, _u32, _vp, _vp]),
     ("cg_de_spatial_grad", _i32, [_shp, _vp, _u64, _vp, _vp]),

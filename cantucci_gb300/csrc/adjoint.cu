@@ -3,6 +3,7 @@
 // (the autograd backward), and the six-evaluation central-difference
 // gradient they replace.
 #include <cmath>
+#include <cstring>
 
 #include "adjoint.cuh"
 #include "common.cuh"
@@ -24,15 +25,20 @@ __device__ __forceinline__ void store8(float* __restrict__ out, uint64_t i, cons
     }
 }
 
+// The reverse-mode gradient of each point; the tape is the dynamic shared
+// memory (adj_tape_bytes(max_iters, CK, blockDim.x) bytes).
+template <int CK, bool FASTREC>
 __global__ void __launch_bounds__(128) k_de_grad(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
                                                  uint64_t n, float* __restrict__ out) {
+    extern __shared__ __align__(16) float4 adj_smem[];
     __shared__ __align__(16) float stage[4][96];
+    const AdjTape tape = adj_tape(adj_smem, s.max_iters, CK);
     const WarpWalk w = warp_walk();
     for (uint64_t base = w.first; base < n; base += w.stride) {
         float x = 0.0f, y = 0.0f, z = 0.0f;
         if (!load_point_warp(pts, n, base, stage[threadIdx.x >> 5], x, y, z)) continue;
         float o[8];
-        polar_de_grad(s, dm.m, x, y, z, o);
+        polar_de_grad<CK, FASTREC>(s, dm.m, x, y, z, tape, o);
         store8(out, base + (threadIdx.x & 31), o);
     }
 }
@@ -84,11 +90,13 @@ __global__ void __launch_bounds__(128) k_de_spatial_grad(ShapeDev s, const float
 __global__ void __launch_bounds__(128) k_de_vjp(ShapeDev s, Dm3 dm, const float* __restrict__ pts,
                                                 const float* __restrict__ g, uint64_t n,
                                                 float* __restrict__ gp, float* __restrict__ params) {
+    extern __shared__ __align__(16) float4 adj_smem[];
+    const AdjTape tape = adj_tape(adj_smem, s.max_iters, ADJ_CK);
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         float o[8];
-        polar_de_grad(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], o);
+        polar_de_grad<ADJ_CK>(s, dm.m, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], tape, o);
         const float gi = g[i];
         if (gp) {
             gp[3 * i] = gi * o[1];
@@ -264,10 +272,42 @@ static cg_status check_grad_shape(const cg_shape* shape) {
         set_error("the adjoint is defined on the real-power polar Mandelbulb (kind 2)");
         return CG_EINVAL;
     }
-    if (shape->max_iters < 1 || shape->max_iters > ADJ_CK * ADJ_MAX_CK) {
-        set_error("adjoint supports 1 <= max_iters <= %d", ADJ_CK * ADJ_MAX_CK);
+    if (shape->max_iters < 1 || shape->max_iters > ADJ_MAX_ITERS) {
+        set_error("adjoint supports 1 <= max_iters <= %d", ADJ_MAX_ITERS);
         return CG_EINVAL;
     }
+    return CG_OK;
+}
+
+// "adjoint_ck": the checkpoint interval of cg_de_grad (5 default, 4 or 8);
+// every interval gives the same outputs.  "adjoint_recompute": 0 (default)
+// recomputes segments with the exact arithmetic, 1 with the fast polar
+// arithmetic (from exact checkpoints; the DE column is exact either way).
+static int g_adjoint_ck = ADJ_CK;
+static int g_adjoint_fastrec = 0;
+
+int set_adjoint_option(const char* name, int64_t v) {
+    if (std::strcmp(name, "adjoint_ck") == 0) {
+        if (v != 4 && v != 5 && v != 8) return 0;
+        g_adjoint_ck = (int)v;
+        return 1;
+    }
+    if (std::strcmp(name, "adjoint_recompute") == 0) {
+        if (v != 0 && v != 1) return 0;
+        g_adjoint_fastrec = (int)v;
+        return 1;
+    }
+    return -1;
+}
+
+template <int CK, bool FR>
+static cg_status launch_de_grad(const ShapeDev& sd, const Dm3& dm, uint32_t max_iters,
+                                const float* points, uint64_t n, float* out, cudaStream_t st) {
+    unsigned G = 0;
+    size_t smem = 0;
+    CG_TRY(adj_launch_shape(k_de_grad<CK, FR>, max_iters, CK, n, &G, &smem));
+    k_de_grad<CK, FR><<<G, 128, smem, st>>>(sd, dm, points, n, out);
+    CG_CHECK_LAUNCH("k_de_grad");
     return CG_OK;
 }
 
@@ -285,10 +325,22 @@ cg_status cg_de_grad(const cg_shape* shape, const float* points, uint64_t n, flo
         return CG_EINVAL;
     }
     if (!n) return CG_OK;
-    k_de_grad<<<grid_for(n, 128, 16), 128, 0, (cudaStream_t)stream>>>(
-        make_shape_dev(*shape), rotation_derivatives(*shape), points, n, out);
-    CG_CHECK_LAUNCH("k_de_grad");
-    return CG_OK;
+    const ShapeDev sd = make_shape_dev(*shape);
+    const Dm3 dm = rotation_derivatives(*shape);
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t N = shape->max_iters;
+    const bool fr = g_adjoint_fastrec != 0;
+    switch (g_adjoint_ck) {
+    case 4:
+        return fr ? launch_de_grad<4, true>(sd, dm, N, points, n, out, st)
+                  : launch_de_grad<4, false>(sd, dm, N, points, n, out, st);
+    case 8:
+        return fr ? launch_de_grad<8, true>(sd, dm, N, points, n, out, st)
+                  : launch_de_grad<8, false>(sd, dm, N, points, n, out, st);
+    default:
+        return fr ? launch_de_grad<ADJ_CK, true>(sd, dm, N, points, n, out, st)
+                  : launch_de_grad<ADJ_CK, false>(sd, dm, N, points, n, out, st);
+    }
 }
 
 cg_status cg_de_grad_tangent(const cg_shape* shape, const float* points, uint64_t n,
@@ -351,12 +403,14 @@ cg_status cg_de_backward(const cg_shape* shape, const float* points, const float
     cudaStream_t st = (cudaStream_t)stream;
     if (grad_params) CG_CUDA(cudaMemsetAsync(grad_params, 0, 4 * sizeof(float), st));
     if (!n) return CG_OK;
-    const unsigned G = grid_for(n, 128, 16);
+    unsigned G = 0;
+    size_t smem = 0;
+    CG_TRY(adj_launch_shape(k_de_vjp, shape->max_iters, ADJ_CK, n, &G, &smem));
     const uint32_t nwarps = G * 4;
     float* partial = nullptr;
     if (grad_params) CG_TRY(acquire_partials((size_t)nwarps * 4, st, &partial));
-    k_de_vjp<<<G, 128, 0, st>>>(make_shape_dev(*shape), rotation_derivatives(*shape), points,
-                                grad_out, n, grad_points, partial);
+    k_de_vjp<<<G, 128, smem, st>>>(make_shape_dev(*shape), rotation_derivatives(*shape), points,
+                                   grad_out, n, grad_points, partial);
     cg_status rs = cuda_status(cudaGetLastError(), "k_de_vjp", __FILE__, __LINE__);
     if (rs == CG_OK && partial) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
     if (partial) {

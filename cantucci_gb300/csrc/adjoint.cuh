@@ -7,11 +7,12 @@
 // For the polar loop one thread returns, per point,
 //   DE, dDE/dp (3), dDE/dpower, dDE/d(euler angles) (3).
 // It is the adjoint of the forward loop, not a finite difference: the
-// forward pass keeps only a checkpoint of (z, dr) every ADJ_CK steps (in
-// registers / L1, never in HBM); the backward pass walks the segments from
-// last to first, recomputes each segment's iterates from its checkpoint and
-// back-propagates through them.  Work is about two forward passes plus one
-// backward pass, whatever max_iters is.
+// forward pass keeps a checkpoint of (z, dr) every CK steps and the step
+// records of its last segment in a per-thread tape in shared memory (never
+// in HBM or local memory); the backward pass walks the segments from last to
+// first, recomputes each earlier segment's iterates from its checkpoint and
+// back-propagates through them.  Work is one forward pass, the recompute of
+// all steps but the last segment's, and one backward pass.
 //
 // Per step k (z_k -> z_{k+1} = r^P u(P theta, P phi) + q, dr_{k+1} =
 // r^(P-1) P dr_k + 1, r = |z_k|, theta = acos(z_z / r), phi = atan2(y, x)):
@@ -28,12 +29,13 @@
 
 #include <cmath>
 
+#include "common.cuh"
 #include "de.cuh"
 
 namespace cg {
 
-constexpr int ADJ_CK = 4;        // checkpoint interval (steps)
-constexpr int ADJ_MAX_CK = 16;   // checkpoints: max_iters <= 64
+constexpr int ADJ_CK = 5;          // default checkpoint interval (steps)
+constexpr int ADJ_MAX_ITERS = 64;  // the longest loop a tape is sized for
 
 // dR/d(angle k) for k = a, b, c, row-major, 3 x 9 floats.
 struct Dm3 {
@@ -74,18 +76,18 @@ struct StepDeriv {
     float t1, zr;            // r^(P-1), r^P
     float sn, cs, sp, cp;    // sin/cos of P theta and P phi
 };
+constexpr int STEP_FIELDS = 13;
 
-// polar_step from `st`, recording the step into `d` (the step never escapes:
-// it is a recompute of a step the forward pass completed).
-__device__ __forceinline__ void polar_step_deriv(const ShapeDev& s, float qx, float qy, float qz,
-                                                 StepState& st, StepDeriv& d) {
+// The step from `st` with |z| = r (not an escape), recorded into `d`: the
+// same operations as polar_step, so the iterate is bit-identical.
+__device__ __forceinline__ void polar_step_rec(const ShapeDev& s, float qx, float qy, float qz,
+                                               float r, StepState& st, StepDeriv& d) {
     d.x = st.x;
     d.y = st.y;
     d.z = st.z;
     d.dr = st.dr;
-    const float P = s.power_f;
-    const float r = magnitude<Exact>(st.x, st.y, st.z);
     d.r = r;
+    const float P = s.power_f;
     d.theta = acosf(__fdiv_rn(st.z, r));
     d.phi = atan2f(st.y, st.x);
     d.t1 = powf(r, __fsub_rn(P, 1.0f));
@@ -98,30 +100,172 @@ __device__ __forceinline__ void polar_step_deriv(const ShapeDev& s, float qx, fl
     st.z = __fadd_rn(__fmul_rn(d.zr, d.cs), qz);
 }
 
+// The same step in the fast polar arithmetic (polar_step_fast: one
+// branch-free arctangent per angle, SFU powers and sin/cos), recorded.  For
+// recomputing a segment from an exact checkpoint: its iterates stay within
+// the fast arithmetic's error of the exact ones over the few steps of a
+// segment.
+__device__ __forceinline__ void polar_step_rec_fast(float P, float qx, float qy, float qz,
+                                                    StepState& st, StepDeriv& d) {
+    d.x = st.x;
+    d.y = st.y;
+    d.z = st.z;
+    d.dr = st.dr;
+    const float rho2 = fmaf(st.x, st.x, st.y * st.y);
+    d.r = sqrtf(fmaf(st.z, st.z, rho2));
+    d.theta = atan2_fast(sqrtf(rho2), st.z);
+    d.phi = atan2_fast(st.y, st.x);
+    const float lr = __log2f(d.r);
+    d.zr = exp2f(P * lr);
+    d.t1 = exp2f((P - 1.0f) * lr);
+    st.dr = fmaf(d.t1 * P, st.dr, 1.0f);
+    sincos_fast(d.theta * P, &d.sn, &d.cs);
+    sincos_fast(d.phi * P, &d.sp, &d.cp);
+    st.x = fmaf(d.zr, d.sn * d.cp, qx);
+    st.y = fmaf(d.zr, d.sp * d.sn, qy);
+    st.z = fmaf(d.zr, d.cs, qz);
+}
+
+// 1/x from the hardware estimate and one Newton step (within an ulp).
+__device__ __forceinline__ float rcp_nr(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return fmaf(fmaf(-x, y, 1.0f), y, y);
+}
+
+// A thread's tape in shared memory: the (z, dr) checkpoint of every CK-th
+// step and the records of one segment of CK steps, field-major
+// ([slot][field][thread]) so that a warp's accesses fall in distinct banks.
+// Shared memory takes run-time slot indices without spilling to local
+// memory.  Bytes per block: adj_tape_bytes.
+struct AdjTape {
+    float4* ck;
+    float* seg;
+    uint32_t tid, nth;
+};
+
+__host__ __device__ constexpr size_t adj_tape_bytes(uint32_t max_iters, int ck, uint32_t nth) {
+    return ((size_t)((max_iters + ck - 1) / ck) * 16u + (size_t)STEP_FIELDS * ck * 4u) * nth;
+}
+
+__device__ __forceinline__ AdjTape adj_tape(void* smem, uint32_t max_iters, int ck) {
+    AdjTape t;
+    t.tid = threadIdx.x;
+    t.nth = blockDim.x;
+    t.ck = reinterpret_cast<float4*>(smem);
+    t.seg = reinterpret_cast<float*>(t.ck + (size_t)((max_iters + ck - 1) / ck) * blockDim.x);
+    return t;
+}
+
+__device__ __forceinline__ void tape_put_ck(const AdjTape& t, uint32_t j, const StepState& st) {
+    t.ck[(size_t)j * t.nth + t.tid] = make_float4(st.x, st.y, st.z, st.dr);
+}
+
+__device__ __forceinline__ StepState tape_get_ck(const AdjTape& t, uint32_t j) {
+    const float4 v = t.ck[(size_t)j * t.nth + t.tid];
+    return StepState{v.x, v.y, v.z, v.w};
+}
+
+__device__ __forceinline__ void tape_put(const AdjTape& t, uint32_t slot, const StepDeriv& d) {
+    float* b = t.seg + (size_t)slot * STEP_FIELDS * t.nth + t.tid;
+    const uint32_t n = t.nth;
+    b[0] = d.x; b[n] = d.y; b[2 * n] = d.z; b[3 * n] = d.dr; b[4 * n] = d.r;
+    b[5 * n] = d.theta; b[6 * n] = d.phi; b[7 * n] = d.t1; b[8 * n] = d.zr;
+    b[9 * n] = d.sn; b[10 * n] = d.cs; b[11 * n] = d.sp; b[12 * n] = d.cp;
+}
+
+__device__ __forceinline__ StepDeriv tape_get(const AdjTape& t, uint32_t slot) {
+    const float* b = t.seg + (size_t)slot * STEP_FIELDS * t.nth + t.tid;
+    const uint32_t n = t.nth;
+    return StepDeriv{b[0], b[n], b[2 * n], b[3 * n], b[4 * n], b[5 * n], b[6 * n],
+                     b[7 * n], b[8 * n], b[9 * n], b[10 * n], b[11 * n], b[12 * n]};
+}
+
+// Launch shape of a kernel with a per-thread tape: block 128, dynamic shared
+// memory for the tape (opting in above 48 KB), and a grid of the blocks
+// that fit on the GPU at once (the kernels walk their points grid-stride).
+template <class Kernel>
+cg_status adj_launch_shape(Kernel kernel, uint32_t max_iters, int ck, uint64_t n,
+                           unsigned* grid, size_t* smem) {
+    *smem = adj_tape_bytes(max_iters, ck, 128);
+    if (*smem > 48 * 1024)
+        CG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)*smem));
+    int per_sm = 0;
+    CG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, *smem));
+    *grid = grid_for(n, 128, (unsigned)(per_sm > 0 ? per_sm : 1));
+    return CG_OK;
+}
+
+// Backward through one recorded step (the step formulas at the top of this
+// file).  `stale` adds the seed of the returned r when the loop ran out and
+// this is its last step.
+__device__ __forceinline__ void polar_back_step(float P, const StepDeriv& z, bool stale,
+                                                float r_seed, float& zbx, float& zby, float& zbz,
+                                                float& drb, float& qbx, float& qby, float& qbz,
+                                                float& Pb) {
+    qbx += zbx;  // the "+ q" of this step
+    qby += zby;
+    qbz += zbz;
+    const float inv_r = rcp_nr(z.r);
+    const float rho2 = z.x * z.x + z.y * z.y;
+    const float lnr = __logf(z.r);
+    const float g_zr = zbx * (z.sn * z.cp) + zby * (z.sn * z.sp) + zbz * z.cs;
+    const float g_th = z.zr * (zbx * (z.cs * z.cp) + zby * (z.cs * z.sp) - zbz * z.sn);
+    const float g_ph = z.zr * z.sn * (zby * z.cp - zbx * z.sp);
+    float rb = g_zr * P * z.t1 + drb * P * z.dr * (P - 1.0f) * z.t1 * inv_r;
+    if (stale) rb += r_seed;
+    Pb += g_zr * z.zr * lnr + g_th * z.theta + g_ph * z.phi + drb * z.dr * z.t1 * (1.0f + P * lnr);
+    drb = drb * P * z.t1;
+    const float thb = P * g_th, phb = P * g_ph;
+    const float rbr = rb * inv_r;
+    float gx = rbr * z.x, gy = rbr * z.y, gz = rbr * z.z;
+    if (rho2 > 1e-30f) {
+        const float inv_rho = rsqrtf(rho2);
+        const float rho = rho2 * inv_rho;
+        const float inv_rho2 = inv_rho * inv_rho;
+        const float inv_r2 = inv_r * inv_r;
+        const float k = thb * z.z * inv_r2 * inv_rho;
+        gx += k * z.x - phb * z.y * inv_rho2;
+        gy += k * z.y + phb * z.x * inv_rho2;
+        gz += -thb * rho * inv_r2;
+    }
+    zbx = gx;
+    zby = gy;
+    zbz = gz;
+}
+
+// DE and its gradient with respect to p, the power and the Euler angles
+// (out[0..7]) by reverse mode over `tape` (adj_tape, sized for
+// s.max_iters <= ADJ_MAX_ITERS).  The forward pass keeps a checkpoint every
+// CK steps and the records of its last segment; the backward pass walks the
+// segments from last to first, recomputing every segment but the last from
+// its checkpoint (FASTREC: in the fast polar arithmetic).
+template <int CK = ADJ_CK, bool FASTREC = false>
 __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __restrict__ dm,
-                                              float px, float py, float pz, float* out) {
+                                              float px, float py, float pz, const AdjTape& tape,
+                                              float* out) {
     float qx, qy, qz;
     rotate_point(s, px, py, pz, qx, qy, qz);
     const float P = s.power_f;
     const uint32_t N = s.max_iters;
 
-    // Forward with checkpoints.
-    StepState ck[ADJ_MAX_CK];
+    // Forward: checkpoints, and every step recorded in its segment slot.
     StepState st = {qx, qy, qz, 1.0f};
     float r = 0.0f;
     uint32_t K = 0;
     bool escaped = false;
     for (uint32_t i = 0; i < N; ++i) {
-        if (i % ADJ_CK == 0) ck[i / ADJ_CK] = st;
-        float ri;
-        const StepState before = st;
-        if (!polar_step(s, qx, qy, qz, st, ri)) {
-            r = ri;
+        if (i % CK == 0) tape_put_ck(tape, i / CK, st);
+        const float ri = magnitude<Exact>(st.x, st.y, st.z);
+        r = ri;
+        if (ri > s.bailout) {
             escaped = true;
-            st = before;
             break;
         }
-        r = ri;
+        StepDeriv d;
+        polar_step_rec(s, qx, qy, qz, ri, st, d);
+        tape_put(tape, i % CK, d);
         ++K;
     }
     // st = z_K (escaped) or z_N; r = |z_K| (escaped) or |z_{N-1}| (stale).
@@ -132,57 +276,37 @@ __device__ __forceinline__ void polar_de_grad(const ShapeDev& s, const float* __
     float drb = -de / dr_fin;
     float zbx = 0.0f, zby = 0.0f, zbz = 0.0f;
     if (escaped && r > 0.0f) {
-        zbx = r_seed * st.x / r;
-        zby = r_seed * st.y / r;
-        zbz = r_seed * st.z / r;
+        const float k = r_seed / r;
+        zbx = k * st.x;
+        zby = k * st.y;
+        zbz = k * st.z;
         r_seed = 0.0f;
     }
     float qbx = 0.0f, qby = 0.0f, qbz = 0.0f, Pb = 0.0f;
 
-    // Backward, segment by segment.  The recompute keeps each step's derived
-    // values (the ones the forward step computes anyway), so the backward
-    // step itself needs no transcendental function but one log.
-    StepDeriv seg[ADJ_CK];
-    const int nseg = (int)((K + ADJ_CK - 1) / ADJ_CK);
-    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
-        const uint32_t k0 = (uint32_t)sgi * ADJ_CK;
-        const uint32_t k1 = min(k0 + ADJ_CK, K);
-        StepState t = ck[sgi];
-        for (uint32_t k = k0; k < k1; ++k) polar_step_deriv(s, qx, qy, qz, t, seg[k - k0]);
-        for (int kk = (int)(k1 - k0) - 1; kk >= 0; --kk) {
-            const uint32_t k = k0 + (uint32_t)kk;
-            const StepDeriv& z = seg[kk];
-            // q gets the "+ q" of this step.
-            qbx += zbx;
-            qby += zby;
-            qbz += zbz;
-            const float rk = z.r;
-            const float rho2 = z.x * z.x + z.y * z.y;
-            const float rho = sqrtf(rho2);
-            const float theta = z.theta, phi = z.phi;
-            const float lnr = logf(rk);
-            const float t1 = z.t1;  // r^(P-1)
-            const float zr = z.zr;  // r^P
-            const float sn = z.sn, cs = z.cs, sp = z.sp, cp = z.cp;
-            const float g_zr = zbx * (sn * cp) + zby * (sn * sp) + zbz * cs;
-            const float g_th = zr * (zbx * (cs * cp) + zby * (cs * sp) - zbz * sn);
-            const float g_ph = zr * sn * (zby * cp - zbx * sp);
-            float rb = g_zr * P * t1 + drb * P * z.dr * (P - 1.0f) * t1 / rk;
-            if (!escaped && k + 1 == N) rb += r_seed;  // stale r belongs to this step
-            Pb += g_zr * zr * lnr + g_th * theta + g_ph * phi +
-                  drb * z.dr * t1 * (1.0f + P * lnr);
-            drb = drb * P * t1;
-            const float thb = P * g_th, phb = P * g_ph;
-            float gx = rb * z.x / rk, gy = rb * z.y / rk, gz = rb * z.z / rk;
-            if (rho > 1e-30f) {
-                const float inv_r2rho = 1.0f / (rk * rk * rho);
-                gx += thb * z.z * z.x * inv_r2rho - phb * z.y / rho2;
-                gy += thb * z.z * z.y * inv_r2rho + phb * z.x / rho2;
-                gz += -thb * rho / (rk * rk);
+    // Backward, segment by segment; the last segment's records are the
+    // forward pass's own.
+    if (K > 0) {
+        const uint32_t last = (K - 1) / CK;
+        for (int j = (int)last; j >= 0; --j) {
+            const uint32_t k0 = (uint32_t)j * CK;
+            const uint32_t k1 = min(k0 + CK, K);
+            if ((uint32_t)j != last) {
+                StepState t = tape_get_ck(tape, (uint32_t)j);
+                for (uint32_t k = k0; k < k1; ++k) {
+                    StepDeriv d;
+                    if (FASTREC)
+                        polar_step_rec_fast(P, qx, qy, qz, t, d);
+                    else
+                        polar_step_rec(s, qx, qy, qz, magnitude<Exact>(t.x, t.y, t.z), t, d);
+                    tape_put(tape, k - k0, d);
+                }
             }
-            zbx = gx;
-            zby = gy;
-            zbz = gz;
+            for (int k = (int)k1 - 1; k >= (int)k0; --k) {
+                const StepDeriv d = tape_get(tape, (uint32_t)k - k0);
+                polar_back_step(P, d, !escaped && (uint32_t)k + 1 == N, r_seed, zbx, zby, zbz,
+                                drb, qbx, qby, qbz, Pb);
+            }
         }
     }
     // z_0 = q.

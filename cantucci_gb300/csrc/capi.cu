@@ -695,6 +695,7 @@ cg_status cg_set_option(const char* name, int64_t value) {
     if (name && set_batch_option(name, value)) return CG_OK;
     if (name && set_trace_option(name, value)) return CG_OK;
     if (name && set_place_option(name, value)) return CG_OK;
+    if (name && set_adjoint_option(name, value) == 1) return CG_OK;
     if (name && strcmp(name, "mesh_graphs") == 0 && (value == 0 || value == 1)) {
         g_mesh_graphs.store((int)value);
         return CG_OK;

@@ -65,6 +65,8 @@ cg_status launch_march(const ShapeDev& s, const float* org, const float* dir, ui
 // cg_set_option knobs of the depth-map march (trace.cu).
 int set_trace_option(const char* name, int64_t v);
 int set_place_option(const char* name, int64_t v);
+// cg_set_option knob of the reverse-mode gradient (adjoint.cu): 1 if taken.
+int set_adjoint_option(const char* name, int64_t v);
 // Shape argument checks of the C ABI (kind, power, max_iters).
 cg_status check_shape(const cg_shape* s);
 

@@ -167,11 +167,14 @@ __global__ void __launch_bounds__(128) k_trace_queue(ShapeDev s, CameraDev c, ui
     }
 }
 
-// Sum over hit pixels of g[i] * dt_i/dtheta.
+// Sum over hit pixels of g[i] * dt_i/dtheta; with cap > 0, pixels whose
+// |dt_i/dtheta_k| exceeds cap for some k are left out.
 __global__ void __launch_bounds__(128) k_trace_backward(ShapeDev s, CameraDev c, Dm3 dm,
                                                         const float* __restrict__ depth,
-                                                        const float* __restrict__ g,
+                                                        const float* __restrict__ g, float cap,
                                                         float* __restrict__ params) {
+    extern __shared__ __align__(16) float4 adj_smem[];
+    const AdjTape tape = adj_tape(adj_smem, s.max_iters, ADJ_CK);
     const uint32_t n = c.width * c.height;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -180,12 +183,21 @@ __global__ void __launch_bounds__(128) k_trace_backward(ShapeDev s, CameraDev c,
         float d[3];
         pixel_ray(c, i, d);
         float o[8];
-        polar_de_grad(s, dm.m, c.eye[0] + t * d[0], c.eye[1] + t * d[1], c.eye[2] + t * d[2], o);
+        polar_de_grad<ADJ_CK>(s, dm.m, c.eye[0] + t * d[0], c.eye[1] + t * d[1],
+                              c.eye[2] + t * d[2], tape, o);
         const float dn = o[1] * d[0] + o[2] * d[1] + o[3] * d[2];
         if (!(fabsf(dn) > 1e-6f)) continue;  // grazing ray: no stable depth derivative
+        float dt[4];
+        bool keep = true;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float v = -gi * o[4 + k] / dn;
+            dt[k] = -o[4 + k] / dn;
+            if (cap > 0.0f && !(fabsf(dt[k]) <= cap)) keep = false;
+        }
+        if (!keep) continue;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v = gi * dt[k];
             if (v == v && fabsf(v) < 1e30f) acc[k] += v;
         }
     }
@@ -297,7 +309,12 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     float* scratch = nullptr;
     CG_TRY(acquire_partials(4, st, &scratch));
     uint32_t* next = reinterpret_cast<uint32_t*>(scratch);
-    CG_CUDA(cudaMemsetAsync(next, 0, sizeof(uint32_t), st));
+    const cudaError_t ze = cudaMemsetAsync(next, 0, sizeof(uint32_t), st);
+    if (ze != cudaSuccess) {  // give the scratch buffer back before reporting
+        const cg_status rr = release_partials(scratch, st);
+        CG_CUDA(ze);
+        return rr;
+    }
     switch (mode_of(s, numerics)) {
     case MODE_P8: launch_trace_queue<MODE_P8>(s, c, max_steps, eps_scale, depth, next, st); break;
     case MODE_INT: launch_trace_queue<MODE_INT>(s, c, max_steps, eps_scale, depth, next, st); break;
@@ -319,11 +336,29 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
     return CG_OK;
 }
 
+cg_status cg_trace_backward_capped(const cg_shape* shape, const cg_camera* camera,
+                                   const float* depth, const float* grad_depth, float cap,
+                                   float* grad_params, void* stream);
+
 cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, const float* depth,
                             const float* grad_depth, float* grad_params, void* stream) {
+    return cg_trace_backward_capped(shape, camera, depth, grad_depth, 0.0f, grad_params, stream);
+}
+
+cg_status cg_trace_backward_capped(const cg_shape* shape, const cg_camera* camera,
+                                   const float* depth, const float* grad_depth, float cap,
+                                   float* grad_params, void* stream) {
     if (!shape || shape->kind != CG_SHAPE_MANDELBULB_POLAR || !depth || !grad_depth ||
         !grad_params) {
         set_error("cg_trace_backward needs the polar shape and device buffers");
+        return CG_EINVAL;
+    }
+    if (shape->max_iters < 1 || shape->max_iters > ADJ_MAX_ITERS) {
+        set_error("cg_trace_backward supports 1 <= max_iters <= %d", ADJ_MAX_ITERS);
+        return CG_EINVAL;
+    }
+    if (!(cap >= 0.0f)) {
+        set_error("cg_trace_backward_capped: cap must be >= 0 (0: no cap)");
         return CG_EINVAL;
     }
     CG_TRY(check_camera(camera));
@@ -333,11 +368,13 @@ cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, cons
     cudaStream_t st = (cudaStream_t)stream;
     CG_CUDA(cudaMemsetAsync(grad_params, 0, 4 * sizeof(float), st));
     const uint64_t n = (uint64_t)c.width * c.height;
-    const unsigned G = grid_for(n, 128, 16);
+    unsigned G = 0;
+    size_t smem = 0;
+    CG_TRY(adj_launch_shape(k_trace_backward, shape->max_iters, ADJ_CK, n, &G, &smem));
     const uint32_t nwarps = G * 4;
     float* partial = nullptr;
     CG_TRY(acquire_partials((size_t)nwarps * 4, st, &partial));
-    k_trace_backward<<<G, 128, 0, st>>>(s, c, dm, depth, grad_depth, partial);
+    k_trace_backward<<<G, 128, smem, st>>>(s, c, dm, depth, grad_depth, cap, partial);
     cg_status rs = cuda_status(cudaGetLastError(), "k_trace_backward", __FILE__, __LINE__);
     if (rs == CG_OK) rs = launch_sum_partials4(partial, nwarps, grad_params, st);
     const cg_status rr = release_partials(partial, st);

@@ -457,6 +457,20 @@ cg_status cg_trace_depth(const cg_shape* shape, const cg_camera* camera, uint32_
 cg_status cg_trace_backward(const cg_shape* shape, const cg_camera* camera, const float* depth,
                             const float* grad_depth, float* grad_params, void* stream);
 
+/* cg_trace_backward with outlier rejection, for fitting (no reference
+ * counterpart).  A hit pixel whose depth derivative |dt/dtheta_k| exceeds
+ * `cap` for any of the four parameters is left out of the sum.  On the
+ * fractal a small share of pixels (a tenth at cap 2 on the power-8.3 map)
+ * carry derivatives of 10^2..10^6: the exact derivative of the f32
+ * estimator along an orbit that the iteration's chaos makes arbitrarily
+ * steep, while the depth itself changes by a small, finite amount over any
+ * step an optimiser takes.  Their sum swamps the rest and points away from
+ * the finite-difference gradient of the loss; without them it agrees with
+ * it (cosine ~0.95).  cap = 0 keeps every pixel, as cg_trace_backward does. */
+cg_status cg_trace_backward_capped(const cg_shape* shape, const cg_camera* camera,
+                                   const float* depth, const float* grad_depth, float cap,
+                                   float* grad_params, void* stream);
+
 /* ---- gradients ---------------------------------------------------------- */
 
 /* Forward + reverse-mode adjoint of the real-power polar estimator
