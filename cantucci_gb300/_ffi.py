@@ -147,7 +147,6 @@ SIGNATURES = [
     ("cg_set_option", _i32, [C.c_char_p, C.c_int64]),
     ("cg_mesher_stream", _i32, [_vp, C.POINTER(_vp)]),
     ("cg_span_grid_work", _i32, [_shp, _spp, _u32, C.POINTER(_u64), C.POINTER(_u64)]),
-    ("cg_fp32_peak_probe", _i32, [_u32, _u32, C.POINTER(C.c_double)]),
 ]
 
 _lib = None

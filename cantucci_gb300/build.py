@@ -26,7 +26,13 @@ LIB = os.path.join(LIB_DIR, "libcantucci_gpu.so")
 CHECKED_LIB = os.path.join(LIB_DIR, "libcantucci_gpu_checked.so")
 
 SOURCES = ["capi.cu", "de_kernels.cu", "mesh.cu", "mesh_batch.cu", "adjoint.cu", "trace.cu", "scan.cu",
-           "probe.cu", "noalloc.cu", "lod.cu"]
+           "noalloc.cu", "lod.cu"]
+# Benchmark instrumentation, outside the C ABI library: the FP32 peak probe
+# (a library of its own) and the native leaf-pool driver (an executable).
+BENCH_SOURCE = os.path.join(CSRC, "bench", "fp32_peak.cu")
+BENCH_LIB = os.path.join(LIB_DIR, "libcantucci_bench.so")
+LEAF_POOL_SOURCE = os.path.join(CSRC, "bench", "leaf_pool.cpp")
+LEAF_POOL_EXE = os.path.join(LIB_DIR, "cg_leaf_pool")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -93,6 +99,58 @@ def build(force: bool = False, verbose: bool = False, checked: bool = False) -> 
     with open(stamp, "w") as f:
         f.write(digest)
     return lib
+
+
+def build_bench(force: bool = False) -> str:
+    """Compile the benchmark's FP32 peak probe into libcantucci_bench.so
+    (not part of the C ABI) and return its path."""
+    h = hashlib.sha256()
+    with open(BENCH_SOURCE, "rb") as f:
+        h.update(f.read())
+    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(os.uname().machine.encode())
+    digest = h.hexdigest()
+    stamp = os.path.join(LIB_DIR, ".digest_bench")
+    if (not force and os.path.exists(BENCH_LIB) and os.path.exists(stamp)
+            and open(stamp).read().strip() == digest):
+        return BENCH_LIB
+    os.makedirs(LIB_DIR, exist_ok=True)
+    tmp = BENCH_LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-shared", BENCH_SOURCE, "-o", tmp, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s%s" % (BENCH_SOURCE, r.stdout, r.stderr))
+    os.replace(tmp, BENCH_LIB)
+    with open(stamp, "w") as f:
+        f.write(digest)
+    return BENCH_LIB
+
+
+def build_leaf_pool(force: bool = False) -> str:
+    """Compile the native leaf-pool driver (T threads, one cg_mesher each,
+    blocking cg_generate_for_box per octree leaf) against the C ABI library
+    and return the executable's path."""
+    lib = build()
+    h = hashlib.sha256()
+    for p in (LEAF_POOL_SOURCE, os.path.join(INCLUDE, "cantucci_gpu.h")):
+        with open(p, "rb") as f:
+            h.update(f.read())
+    h.update(os.uname().machine.encode())
+    digest = h.hexdigest()
+    stamp = os.path.join(LIB_DIR, ".digest_leaf_pool")
+    if (not force and os.path.exists(LEAF_POOL_EXE) and os.path.exists(stamp)
+            and open(stamp).read().strip() == digest):
+        return LEAF_POOL_EXE
+    tmp = LEAF_POOL_EXE + ".tmp%d" % os.getpid()
+    cmd = [nvcc(), "-O2", "-std=c++17", LEAF_POOL_SOURCE, "-I", INCLUDE, "-L", LIB_DIR,
+           "-lcantucci_gpu", "-Xlinker", "-rpath," + os.path.dirname(lib), "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s%s" % (LEAF_POOL_SOURCE, r.stdout, r.stderr))
+    os.replace(tmp, LEAF_POOL_EXE)
+    with open(stamp, "w") as f:
+        f.write(digest)
+    return LEAF_POOL_EXE
 
 
 if __name__ == "__main__":

@@ -1,13 +1,15 @@
-// probe.cu -- FP32 pipe peak of the current GPU, measured: the roofline
-// denominator for the distance-estimator kernels (which run on the FP32 and
-// SFU pipes, not on tensor cores).
+// fp32_peak.cu -- FP32 pipe peak of the current GPU, measured: the roofline
+// denominator of the distance-estimator kernels, which run on the FP32 and
+// SFU pipes, not on tensor cores.  Benchmark instrumentation: built into
+// libcantucci_bench.so for bench.py, not part of the C ABI.
 //
 // Every thread runs 8 independent FFMA chains, 8 warps per scheduler, one
 // full wave of CTAs per SM; the result is 2 flops per FFMA over the kernel's
 // CUDA-event time.
-#include "common.cuh"
+#include <cstdint>
+#include <cuda_runtime.h>
 
-namespace cg {
+namespace cgb {
 
 __global__ void __launch_bounds__(256) k_ffma_peak(float* out, uint32_t iters, float a, float b) {
     float r0 = threadIdx.x * 1e-7f, r1 = r0 + 1e-7f, r2 = r0 + 2e-7f, r3 = r0 + 3e-7f;
@@ -53,25 +55,26 @@ __global__ void __launch_bounds__(256) k_ffma2_peak(float* out, uint32_t iters, 
     if (s == 0x123456789ull) out[blockIdx.x] = 1.0f;  // keeps the chains alive
 }
 
-}  // namespace cg
+}  // namespace cgb
 
-using namespace cg;
+using namespace cgb;
 
-extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, uint32_t packed, double* flops_per_s) {
-    if (!flops_per_s || iters == 0) {
-        set_error("bad arguments");
-        return CG_EINVAL;
-    }
+// FP32 flop/s of the current device (2 per FMA), from `iters` x 128 FMA per
+// thread; packed != 0 issues them as two-lane fma.rn.f32x2.  Returns 0, or
+// the CUDA error code.
+extern "C" int cgb_fp32_peak(uint32_t iters, uint32_t packed, double* flops_per_s) {
+    if (!flops_per_s || iters == 0) return (int)cudaErrorInvalidValue;
+    int dev = 0, sms = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (err != cudaSuccess) return (int)err;
+    const unsigned blocks = (unsigned)sms * 8, threads = 256;
     float* out = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    const unsigned blocks = (unsigned)sm_count() * 8, threads = 256;
-    cg_status st = CG_OK;
     do {
-        if ((st = cuda_status(cudaMalloc(&out, blocks * sizeof(float)), "cudaMalloc", __FILE__,
-                              __LINE__)) != CG_OK)
-            break;
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
+        if ((err = cudaMalloc(&out, blocks * sizeof(float))) != cudaSuccess) break;
+        if ((err = cudaEventCreate(&e0)) != cudaSuccess) break;
+        if ((err = cudaEventCreate(&e1)) != cudaSuccess) break;
         for (int rep = 0; rep < 2; ++rep) {  // rep 0 warms up
             if (rep) cudaEventRecord(e0);
             const uint32_t it = rep ? iters : iters / 8 + 1;
@@ -81,8 +84,7 @@ extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, uint32_t packed, double*
                 k_ffma_peak<<<blocks, threads>>>(out, it, 0.999999f, 1e-7f);
         }
         cudaEventRecord(e1);
-        if ((st = cuda_status(cudaEventSynchronize(e1), "k_ffma_peak", __FILE__, __LINE__)) != CG_OK)
-            break;
+        if ((err = cudaEventSynchronize(e1)) != cudaSuccess) break;
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
         const double fmas = (double)blocks * threads * iters * 16.0 * 8.0;
@@ -91,5 +93,5 @@ extern "C" cg_status cg_fp32_peak_probe(uint32_t iters, uint32_t packed, double*
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (out) cudaFree(out);
-    return st;
+    return (int)err;
 }

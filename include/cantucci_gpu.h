@@ -552,11 +552,6 @@ cg_status cg_mesher_stream(cg_mesher* mesher, void** stream);
 cg_status cg_span_grid_work(const cg_shape* shape, const cg_span* span, uint32_t resolution,
                             uint64_t* steps, uint64_t* escapes);
 
-/* FP32 pipe peak of the current device in flop/s (2 per FMA), measured with
- * independent FMA chains, `iters` x 128 FMA per thread; packed != 0 issues
- * them as two-lane fma.rn.f32x2.  No reference counterpart: the denominator
- * of the estimator's roofline. */
-cg_status cg_fp32_peak_probe(uint32_t iters, uint32_t packed, double* flops_per_s);
 
 #ifdef __cplusplus
 }
