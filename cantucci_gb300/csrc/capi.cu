@@ -121,7 +121,7 @@ cg_status check_shape(const cg_shape* s) {
 // generate_for_box's assertions (src/mesh/buffer.rs:35-39) plus
 // GridTable::fill_with's size >= 2 (src/util/grid.rs:24); res <= 1024 keeps
 // every grid index in 32 bits.
-static cg_status check_span_res(const cg_span* span, uint32_t res) {
+cg_status check_span_res(const cg_span* span, uint32_t res) {
     if (!span) {
         set_error("span is NULL");
         return CG_EINVAL;

@@ -69,6 +69,8 @@ int set_place_option(const char* name, int64_t v);
 int set_adjoint_option(const char* name, int64_t v);
 // Shape argument checks of the C ABI (kind, power, max_iters).
 cg_status check_shape(const cg_shape* s);
+// Span and resolution checks of the meshing entry points (capi.cu).
+cg_status check_span_res(const cg_span* span, uint32_t res);
 
 // Counters the mesher kernels write on the device.
 struct MeshCounters {

@@ -1,8 +1,6 @@
 // noalloc.cu -- span meshing without any device allocation.
 //
 // Some callers cannot call cudaMalloc at the point where they mesh a span:
-//   * code that runs while a stream is being captured into a CUDA graph
-//     (allocation is not a capturable operation);
 //   * engines and frameworks whose own caching allocator has already reserved
 //     the device memory and forbids other allocations after start-up;
 //   * real-time loops (a renderer's per-frame LOD update, as cantucci's
@@ -19,10 +17,13 @@
 // the symbol is only a stand-in, not a device address; the device address is
 // looked up with cudaGetSymbolAddress, once per device, on the first call
 // made with that device current.  That first call should therefore come
-// before any stream capture.  All calls share the one array: two calls whose
-// work overlaps on the GPU (different streams, or different host threads)
-// race on it and must be serialised by the caller.  Everything the kernels
-// read before writing (the mesh counters) is cleared by each call.
+// before any stream capture.  The address is valid for the life of the
+// device's primary context: a cudaDeviceReset unloads the module, and the
+// cached address then no longer names the array.  All calls share the one
+// array: two calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it and must be serialised by the caller.
+// Everything the kernels read before writing (the mesh counters) is cleared
+// by each call.
 #include <mutex>
 
 #include "common.cuh"
@@ -73,31 +74,13 @@ extern "C" cg_status cg_generate_for_box_noalloc(const cg_span* span, const cg_s
         set_error("NULL argument");
         return CG_EINVAL;
     }
-    for (int k = 0; k < 3; ++k) {
-        if (!(span->start[k] < span->end[k])) {
-            set_error("span.start[%d] < span.end[%d] does not hold", k, k);
-            return CG_EINVAL;
-        }
-    }
-    if (resolution < 2 || (resolution & (resolution - 1)) != 0 ||
-        resolution > NOALLOC_MAX_RES) {
+    // the allocating entry point's checks, then the fixed workspace's cap
+    CG_TRY(check_span_res(span, resolution));
+    CG_TRY(check_shape(shape));
+    if (resolution > NOALLOC_MAX_RES) {
         set_error("cg_generate_for_box_noalloc: resolution %u must be a power of two in [2, %u] "
                   "(its fixed workspace is %zu bytes)",
                   resolution, NOALLOC_MAX_RES, NOALLOC_SCRATCH_BYTES);
-        return CG_EINVAL;
-    }
-    if (shape->kind == CG_SHAPE_MANDELBULB && (shape->power < 0 || shape->power > 255)) {
-        set_error("Mandelbulb power %d outside the u8 range", shape->power);
-        return CG_EINVAL;
-    }
-    if ((shape->kind == CG_SHAPE_MANDELBULB || shape->kind == CG_SHAPE_MANDELBULB_POLAR) &&
-        shape->max_iters < 1) {
-        set_error("max_iters must be >= 1");
-        return CG_EINVAL;
-    }
-    if (shape->kind != CG_SHAPE_MANDELBULB && shape->kind != CG_SHAPE_SPHERE &&
-        shape->kind != CG_SHAPE_MANDELBULB_POLAR) {
-        set_error("unknown shape kind %d", shape->kind);
         return CG_EINVAL;
     }
     const size_t need = mesh_workspace_layout(resolution, nullptr, nullptr);

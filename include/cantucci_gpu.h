@@ -206,20 +206,26 @@ cg_status cg_generate_for_box_device(cg_mesher* mesher, const cg_span* span,
                                      uint64_t index_cap, uint64_t* n_vertices,
                                      uint64_t* n_indices, cg_timings* timings);
 
-/* generate_for_box for callers that must not allocate device memory: code
- * running under CUDA-graph stream capture, engines whose allocator owns all
- * device memory, and per-frame LOD loops that cannot take cudaMalloc's
- * synchronisation.  No counterpart in the reference (which allocates Vecs per
- * call).  Uses a fixed 3 MiB __device__ workspace inside the library instead
- * of a cg_mesher, so resolution is limited to 64 (cantucci's leaf resolution,
- * src/mesh/mod.rs:133); larger values return CG_EINVAL.  Every GPU that loads
- * the library holds the 3 MiB until exit.  The first call on a device looks
- * the workspace up (cudaGetSymbolAddress) and should come before any stream
- * capture.  All calls share the workspace: calls that overlap on the GPU race,
- * so serialise them.  Asynchronous on `stream`: vertices/indices (DEVICE, up
- * to their capacities) and counts (DEVICE, 3 x uint32: vertices, quads,
- * status bit 0 = a lerp factor left [0,1]) are valid once the stream reaches
- * this point; indices hold 6 x quads entries. */
+/* generate_for_box for callers that must not allocate device memory:
+ * engines whose own allocator owns all device memory, and per-frame LOD
+ * loops that cannot take cudaMalloc's synchronisation.  No counterpart in the
+ * reference (which allocates Vecs per call).  Uses a fixed 3 MiB __device__
+ * workspace inside the library instead of a cg_mesher, so resolution is
+ * limited to 64 (cantucci's leaf resolution, src/mesh/mod.rs:133); larger
+ * values return CG_EINVAL, and spans and shapes are checked as
+ * cg_generate_for_box checks them.  Every GPU that loads the library holds
+ * the 3 MiB until exit.  The first call on a device looks the workspace up
+ * (cudaGetSymbolAddress) and should come before any stream capture; the
+ * address is kept for the life of the device's primary context (after a
+ * cudaDeviceReset, load the library anew).  All calls share the workspace:
+ * calls that overlap on the GPU race, so serialise them.  Asynchronous on
+ * `stream`: counts (DEVICE, 3 x uint32: vertices, quads, status bit 0 = a
+ * lerp factor left [0,1], where the reference panics) and the mesh are valid
+ * once the stream reaches this point.  The mesh is cut at the capacities:
+ * min(counts[0], vertex_cap) vertices and min(6 counts[1], index_cap)
+ * indices are written, nothing beyond, and the call still returns CG_OK, so
+ * the caller compares counts[0] with vertex_cap and 6 counts[1] with
+ * index_cap (and tests bit 0 of counts[2]) before using the mesh. */
 cg_status cg_generate_for_box_noalloc(const cg_span* span, const cg_shape* shape,
                                       uint32_t resolution, cg_vertex* vertices,
                                       uint64_t vertex_cap, uint32_t* indices, uint64_t index_cap,
