@@ -64,6 +64,10 @@ def lib():
                                            C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
                                            C.c_uint64, u64p, u64p, C.c_void_p]
         L.orc_generate_for_box.restype = C.c_int
+        L.orc_mesh_from_dists.argtypes = [sp, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                                          C.c_uint64, u64p, u64p]
+        L.orc_mesh_from_dists.restype = C.c_int
         L.orc_march.argtypes = [sp, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_float,
                                 C.c_void_p, C.c_void_p, C.c_int]
         L.orc_create_spans.argtypes = [C.c_void_p, C.c_void_p]
@@ -326,6 +330,26 @@ def generate_for_box(shape: Shape, span, res: int, nthreads=None, want_grids=Fal
         out["dists"] = dists.reshape(N, N, N)
         out["points"] = points.reshape(res, res, res)
     return out
+
+
+def mesh_from_dists(shape: Shape, span, res: int, dists, nthreads=None, vcap=None, icap=None):
+    """Steps 2-3 of generate_for_box on the given (res+1)^3 corner distances.
+    Returns dict(rc, nv, ni, vertices, indices, points)."""
+    sp = _f32(span).reshape(6)
+    d = _f32(dists).reshape(-1)
+    assert d.size == (res + 1) ** 3
+    points = np.empty(res ** 3, np.uint32)
+    vcap = res ** 3 if vcap is None else vcap
+    icap = 18 * res ** 3 if icap is None else icap
+    verts = np.empty(vcap, VERTEX_DTYPE)
+    idx = np.empty(icap, np.uint32)
+    nv, ni = C.c_uint64(), C.c_uint64()
+    rc = lib().orc_mesh_from_dists(C.byref(shape), sp.ctypes.data, res,
+                                   nthreads or default_threads(), d.ctypes.data,
+                                   points.ctypes.data, verts.ctypes.data, vcap, idx.ctypes.data,
+                                   icap, C.byref(nv), C.byref(ni))
+    return dict(rc=rc, nv=nv.value, ni=ni.value, vertices=verts[:nv.value].copy(),
+                indices=idx[:ni.value].copy(), points=points.reshape(res, res, res))
 
 
 def march(shape: Shape, origins, dirs, max_steps=100, epsilon=1e-6, nthreads=None):

@@ -976,8 +976,10 @@ static void mesh_quads_write(void* vctx, uint64_t b, uint64_t e) {
 
 static int is_pow2(uint32_t v) { return v && !(v & (v - 1)); }
 
-int orc_generate_for_box(const orc_shape* s, const float span[6], uint32_t res, int nthreads,
-                         float* dists_out, uint32_t* points_out,
+/* generate_for_box, or with `dists_in` steps 2 and 3 only, on those corner
+ * distances instead of step 1's. */
+static int generate_impl(const orc_shape* s, const float span[6], uint32_t res, int nthreads,
+                         const float* dists_in, float* dists_out, uint32_t* points_out,
                          orc_vertex* verts, uint64_t vcap, uint32_t* idx, uint64_t icap,
                          uint64_t* nv, uint64_t* ni, double timings_ms[3]) {
     /* generate_for_box asserts (buffer.rs:35-39); GridTable::fill_with(res)
@@ -1008,14 +1010,15 @@ int orc_generate_for_box(const orc_shape* s, const float span[6], uint32_t res, 
     const uint64_t ncorner = (uint64_t)c.N * c.N * c.N;
     const uint64_t ncell = (uint64_t)res * res * res;
 
-    c.dists = dists_out ? dists_out : (float*)malloc(ncorner * sizeof(float));
+    c.dists = dists_in ? (float*)dists_in
+                       : (dists_out ? dists_out : (float*)malloc(ncorner * sizeof(float)));
     c.surf = (uint8_t*)malloc(ncell);
     c.points = points_out ? points_out : (uint32_t*)malloc(ncell * sizeof(uint32_t));
     c.row_quads = (uint64_t*)calloc(res, sizeof(uint64_t));
     c.slab_off = (uint64_t*)calloc(res + 1, sizeof(uint64_t));
 
     double t0 = now_ms();
-    parallel_for(ncorner, 4096, nthreads, mesh_step1, &c);
+    if (!dists_in) parallel_for(ncorner, 4096, nthreads, mesh_step1, &c);
     double t1 = now_ms();
 
     parallel_for(ncell, 1 << 16, nthreads, mesh_surface, &c);
@@ -1048,12 +1051,28 @@ int orc_generate_for_box(const orc_shape* s, const float span[6], uint32_t res, 
     if (c.lerp_fail) rc = ORC_ELERP;
     else if ((verts && v > vcap) || (idx && q > icap)) rc = ORC_ECAPACITY;
 
-    if (!dists_out) free(c.dists);
+    if (!dists_in && !dists_out) free(c.dists);
     if (!points_out) free(c.points);
     free(c.surf);
     free(c.row_quads);
     free(c.slab_off);
     return rc;
+}
+
+int orc_generate_for_box(const orc_shape* s, const float span[6], uint32_t res, int nthreads,
+                         float* dists_out, uint32_t* points_out,
+                         orc_vertex* verts, uint64_t vcap, uint32_t* idx, uint64_t icap,
+                         uint64_t* nv, uint64_t* ni, double timings_ms[3]) {
+    return generate_impl(s, span, res, nthreads, NULL, dists_out, points_out, verts, vcap, idx,
+                         icap, nv, ni, timings_ms);
+}
+
+int orc_mesh_from_dists(const orc_shape* s, const float span[6], uint32_t res, int nthreads,
+                        const float* dists, uint32_t* points_out, orc_vertex* verts,
+                        uint64_t vcap, uint32_t* idx, uint64_t icap, uint64_t* nv, uint64_t* ni) {
+    if (!dists) return ORC_EINVAL;
+    return generate_impl(s, span, res, nthreads, dists, NULL, points_out, verts, vcap, idx, icap,
+                         nv, ni, NULL);
 }
 
 /* ------------------------------------------------------------------ */

@@ -93,6 +93,14 @@ int orc_generate_for_box(const orc_shape* s, const float span[6], uint32_t res, 
                          orc_vertex* verts, uint64_t vcap, uint32_t* idx, uint64_t icap,
                          uint64_t* nv, uint64_t* ni, double timings_ms[3]);
 
+/* Steps 2 and 3 of the same mesher (buffer.rs:85-372) on GIVEN corner
+ * distances `dists` ((res+1)^3 floats, GridTable order) instead of step 1's:
+ * the surface cells, vertex positions and quads follow from the distances
+ * alone, so a mesher fed the same distances must place the same bits. */
+int orc_mesh_from_dists(const orc_shape* s, const float span[6], uint32_t res, int nthreads,
+                        const float* dists, uint32_t* points, orc_vertex* verts, uint64_t vcap,
+                        uint32_t* idx, uint64_t icap, uint64_t* nv, uint64_t* ni);
+
 /* ---- sphere tracing: ShapeMesh::get_focii march loop (src/mesh/mod.rs:229-241) ---- */
 void orc_march(const orc_shape* s, const float* origins, const float* dirs, uint64_t n,
                uint32_t max_steps, float epsilon, float* hits, uint8_t* hit, int nthreads);
