@@ -1084,9 +1084,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="step-1 kernel: 0 auto (2x4x4 bricks), 1 linear, 2 bricks, 3 packed "
-                         "f32x2 (all bit-identical)")
+                         "f32x2, 4 bricks at 48 registers (all bit-identical)")
     ap.add_argument("--fit-steps", type=int, default=300,
                     help="Adam steps of the depth-map fit extra")
     ap.add_argument("--only-extra", default=None,
