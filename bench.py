@@ -1003,7 +1003,7 @@ def run_ours(args, rank, world, local_rank):
     roofline = {
         "bound": "fp32",
         "kernel": {0: "k_de_grid_brick", 1: "k_de_grid", 2: "k_de_grid_brick",
-                   3: "k_de_grid_p8x2"}[args.de_kernel],
+                   3: "k_de_grid_p8x2", 4: "k_de_grid_brick_48reg"}[args.de_kernel],
         "achieved": achieved, "peak": peak_tf,
         "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
         "peak_source": "measured in this run: FFMA chains, 2 flop per FFMA (FP32 pipe peak; "
