@@ -32,11 +32,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libref_shader.so")
-# The cantucci source tree (CANTUCCI_REFERENCE, else the build container's
-# read-only copy at /root/reference); the recipe does nothing without it.
-DEFAULT_REFERENCE = "/root/reference"
-REFERENCE = os.environ.get("CANTUCCI_REFERENCE") or (
-    DEFAULT_REFERENCE if os.path.isdir(os.path.join(DEFAULT_REFERENCE, "src")) else None)
+# The cantucci source tree; the recipe does nothing without it.
+REFERENCE = os.environ.get("CANTUCCI_REFERENCE")
 SHADERS = {"mandelbulb": "src/shape/mandelbulb.frag", "sphere": "src/shape/shape.frag"}
 
 # (name, kind, parameters).  Mandelbulb: power (integer), max_iters, bailout.

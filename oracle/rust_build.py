@@ -117,12 +117,7 @@ class TranslateError(Exception):
 
 
 def reference_root():
-    """CANTUCCI_REFERENCE, else the build container's read-only copy."""
-    env = os.environ.get("CANTUCCI_REFERENCE")
-    if env:
-        return env
-    default = "/root/reference"
-    return default if os.path.isdir(os.path.join(default, "src")) else None
+    return os.environ.get("CANTUCCI_REFERENCE")
 
 
 def available() -> bool:
