@@ -1003,7 +1003,7 @@ def run_ours(args, rank, world, local_rank):
     roofline = {
         "bound": "fp32",
         "kernel": {0: "k_de_grid_brick", 1: "k_de_grid", 2: "k_de_grid_brick",
-                   3: "k_de_grid_p8x2", 4: "k_de_grid_brick_48reg"}[args.de_kernel],
+                   3: "k_de_grid_p8x2"}[args.de_kernel],
         "achieved": achieved, "peak": peak_tf,
         "unit": "TFLOP/s", "frac": achieved / peak_tf, "traffic": None,
         "peak_source": "measured in this run: FFMA chains, 2 flop per FFMA (FP32 pipe peak; "
@@ -1084,9 +1084,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3, 4],
+    ap.add_argument("--de-kernel", type=int, default=0, choices=[0, 1, 2, 3],
                     help="step-1 kernel: 0 auto (2x4x4 bricks), 1 linear, 2 bricks, 3 packed "
-                         "f32x2, 4 bricks at 48 registers (all bit-identical)")
+                         "f32x2 (all bit-identical)")
     ap.add_argument("--fit-steps", type=int, default=300,
                     help="Adam steps of the depth-map fit extra")
     ap.add_argument("--only-extra", default=None,

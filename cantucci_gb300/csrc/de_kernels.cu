@@ -72,11 +72,9 @@ __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* _
 // collects its row's 4 bits per brick and stores the finished word once (no
 // atomics; every word is written, padding bits 0).  With group 1 (smaller
 // grids, where 8-brick units would leave SMs idle) each brick's 4 bits go
-// into the word with atomicOr (sgn zeroed first).  MINB is the launch
-// bounds' blocks per SM: 1 lets ptxas take the registers it wants (72 for
-// Mandelbulb<8> unrolled, 3 resident blocks), 5 caps them at 48 for 5 blocks.
-template <int M, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_de_grid_brick(ShapeDev s, GridDev g,
+// into the word with atomicOr (sgn zeroed first).
+template <int M>
+__global__ void __launch_bounds__(256) k_de_grid_brick(ShapeDev s, GridDev g,
                                                        float* __restrict__ out,
                                                        uint32_t* __restrict__ sgn, uint32_t W,
                                                        uint32_t group,
@@ -315,7 +313,7 @@ static int g_de_grid_kernel = DE_GRID_AUTO;
 int de_grid_kernel_option() { return g_de_grid_kernel; }
 
 int set_de_grid_kernel(int v) {
-    if (v < DE_GRID_AUTO || v > DE_GRID_BRICK5) return 0;
+    if (v < DE_GRID_AUTO || v > DE_GRID_PACKED) return 0;
     g_de_grid_kernel = v;
     return 1;
 }
@@ -337,12 +335,7 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
         const uint64_t units8 = rows * ((bz + 7) / 8);
         const uint32_t group = units8 >= 4ull * sm_count() * 8 * (B / 32) ? 8u : 1u;
         const uint64_t units = rows * ((bz + group - 1) / group);
-        if (k == DE_GRID_BRICK5)
-            k_de_grid_brick<M, 5><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W,
-                                                                            group, gp);
-        else
-            k_de_grid_brick<M, 1><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W,
-                                                                            group, gp);
+        k_de_grid_brick<M><<<grid_for(units * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, group, gp);
     } else {
         const uint64_t total = (uint64_t)g.n * g.n * g.n;
         k_de_grid<M><<<grid_for(total, B, 8), B, 0, st>>>(s, g, out, sgn, W, gp);

@@ -34,8 +34,7 @@ cg_status launch_de_points(const ShapeDev& s, const float* pts, uint64_t n, floa
 int set_batch_option(const char* name, int64_t v);
 
 // Step-1 kernel variants (cg_set_option "de_grid_kernel").
-enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3,
-       DE_GRID_BRICK5 = 4 };
+enum { DE_GRID_AUTO = 0, DE_GRID_LINEAR = 1, DE_GRID_BRICK = 2, DE_GRID_PACKED = 3 };
 #ifdef CG_CHECKED
 // Out-of-range counters of each checked translation unit (common.cuh).
 void oob_read_mesh(uint64_t* count, uint32_t* line, bool reset);

@@ -528,8 +528,7 @@ cg_status cg_fd_grad(const cg_shape* shape, const float* points, uint64_t n, flo
 
 /* Process-wide tuning knobs.  "de_grid_kernel": 0 auto, 1 one corner per
  * thread in GridTable order, 2 2x4x4 bricks per warp, 3 (P=8 only) one
- * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic,
- * 4 the bricks of 2 with registers capped for 5 resident blocks per SM.
+ * 4x4x4 brick per warp, two corners per thread with packed f32x2 arithmetic.
  * "place_blocks_per_sm" (1..1024, default 128): the vertex placement's grid.
  * "side_stream_priority" (1 default, or 0): whether meshers created
  * afterwards run their quads and copies on a highest-priority stream.
