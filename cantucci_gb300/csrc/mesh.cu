@@ -234,6 +234,12 @@ __global__ void __launch_bounds__(256) k_quad_count(const uint32_t* __restrict__
         CG_AT(quadcnt, r, rows) = quad_count_row(sgn, d, r);
 }
 
+// Warp-cooperative quad emission: a row's Wc sign words (res <= 1024, so Wc
+// is a power of two <= 32) go to Wc lanes, 32 / Wc rows per warp.  Each lane
+// counts its word's quads, a segmented scan over the row's lanes gives the
+// word's first quad, and the lane writes them: the same list as one thread
+// per row walking the words in order, with the row's quads spread over its
+// lanes and their stores side by side.
 __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ sgn, MeshDims d,
                                                    const float* __restrict__ dists,
                                                    const uint32_t* __restrict__ cellbits,
@@ -242,10 +248,26 @@ __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ 
                                                    const uint32_t* __restrict__ quadoff,
                                                    uint32_t* __restrict__ idx, uint64_t icap) {
     const uint32_t rows = d.res * d.res;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-         r += gridDim.x * blockDim.x)
-        quad_emit_row(sgn, d, dists, cellbits, wordoff, rowoff, 0u, CG_AT(quadoff, r, rows), idx,
-                      icap, r);
+    const uint32_t L = d.Wc, per_warp = 32 / L;
+    const uint32_t lane = threadIdx.x & 31, sub = lane % L;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t r0 = warp * per_warp; r0 < rows; r0 += nwarps * per_warp) {
+        const uint32_t r = r0 + lane / L;
+        const bool ok = r < rows;
+        const uint32_t x = ok ? r / d.res : 0u, y = ok ? r % d.res : 0u;
+        EdgeWords e = {0u, 0u, 0u};
+        if (ok) e = edge_words(sgn, d, x, y, sub);
+        const uint32_t cnt = __popc(e.ex) + __popc(e.ey) + __popc(e.ez);
+        uint32_t inc = cnt;
+        for (uint32_t o = 1; o < L; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, L);
+            if (sub >= o) inc += v;
+        }
+        if (ok && cnt)
+            quad_emit_word(e, d, dists, cellbits, wordoff, rowoff, 0u,
+                           (uint64_t)CG_AT(quadoff, r, rows) + (inc - cnt), idx, icap, x, y, sub);
+    }
 }
 
 // Copy of the first n words of src (n <= src_cap) to dst (n <= dst_cap),
@@ -502,8 +524,8 @@ static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStr
 
 static cg_status launch_quad_emit(const MeshDims& d, const MeshWork& w, uint32_t* idx,
                                   uint64_t icap, cudaStream_t st) {
-    const uint32_t rows = d.res * d.res;
-    const unsigned B = 256, G = grid_for(rows, B, 8);
+    const uint64_t lanes = (uint64_t)d.res * d.res * d.Wc;
+    const unsigned B = 256, G = grid_for(lanes, B, 8);
     k_quad_emit<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff, w.quadoff,
                                  idx, icap);
     CG_CHECK_LAUNCH("k_quad_emit");

@@ -413,9 +413,64 @@ __device__ __forceinline__ uint32_t vertex_id(const MeshDims& d, const uint32_t*
            __popc(CG_AT(cellbits, r * d.Wc + w, nc) & ((1u << b) - 1u));
 }
 
-// Quad indices of corner row r (buffer.rs:288-372): corner order, then +x,
-// +y, +z; winding by dists[(x, y, z)] < 0.0.  Vertex ids are rowoff-based
-// minus `vbase`; quads are written from index 6 * q (capacity icap).
+// Quad indices of corner row (x, y), sign word w (buffer.rs:288-372), from
+// quad q on: corner order, then +x, +y, +z; winding by dists[(x, y, z)] <
+// 0.0.  Vertex ids are rowoff-based minus `vbase`; quad q is written from
+// index 6 * q (capacity icap).  Returns the next quad.
+__device__ __forceinline__ uint64_t quad_emit_word(const EdgeWords& e, const MeshDims& d,
+                                                   const float* __restrict__ dists,
+                                                   const uint32_t* __restrict__ cellbits,
+                                                   const uint32_t* __restrict__ wordoff,
+                                                   const uint32_t* __restrict__ rowoff,
+                                                   uint32_t vbase, uint64_t q,
+                                                   uint32_t* __restrict__ idx, uint64_t icap,
+                                                   uint32_t x, uint32_t y, uint32_t w) {
+    uint32_t any = e.ex | e.ey | e.ez;
+    while (any) {
+        const uint32_t b = __ffs(any) - 1;
+        any &= any - 1;
+        const uint32_t z = w * 32 + b;
+        const bool neg = CG_AT(dists, ((size_t)x * d.n + y) * d.n + z, (uint64_t)d.n * d.n * d.n) < 0.0f;
+        const uint32_t bit = 1u << b;
+        uint32_t t[6];
+        if (e.ex & bit) {
+            const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z - 1) - vbase;
+            const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
+            const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
+            const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+            if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+            else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+            if (6 * q + 6 <= icap)
+                for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
+            ++q;
+        }
+        if (e.ey & bit) {
+            const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z - 1) - vbase;
+            const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
+            const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
+            const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+            if (neg) { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+            else     { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+            if (6 * q + 6 <= icap)
+                for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
+            ++q;
+        }
+        if (e.ez & bit) {
+            const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y - 1, z) - vbase;
+            const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
+            const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
+            const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
+            if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
+            else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
+            if (6 * q + 6 <= icap)
+                for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
+            ++q;
+        }
+    }
+    return q;
+}
+
+// The quads of corner row r, one word after another from quad q.
 __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                               const float* __restrict__ dists,
                                               const uint32_t* __restrict__ cellbits,
@@ -424,51 +479,9 @@ __device__ __forceinline__ void quad_emit_row(const uint32_t* __restrict__ sgn, 
                                               uint64_t q, uint32_t* __restrict__ idx, uint64_t icap,
                                               uint32_t r) {
     const uint32_t x = r / d.res, y = r % d.res;
-    for (uint32_t w = 0; w < d.Wc; ++w) {
-        const EdgeWords e = edge_words(sgn, d, x, y, w);
-        uint32_t any = e.ex | e.ey | e.ez;
-        while (any) {
-            const uint32_t b = __ffs(any) - 1;
-            any &= any - 1;
-            const uint32_t z = w * 32 + b;
-            const bool neg = CG_AT(dists, ((size_t)x * d.n + y) * d.n + z, (uint64_t)d.n * d.n * d.n) < 0.0f;
-            const uint32_t bit = 1u << b;
-            uint32_t t[6];
-            if (e.ex & bit) {
-                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z - 1) - vbase;
-                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
-                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
-                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
-                if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
-                else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
-                if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
-                ++q;
-            }
-            if (e.ey & bit) {
-                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z - 1) - vbase;
-                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
-                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z - 1) - vbase;
-                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
-                if (neg) { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
-                else     { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
-                if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
-                ++q;
-            }
-            if (e.ez & bit) {
-                const uint32_t v0 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y - 1, z) - vbase;
-                const uint32_t v1 = vertex_id(d, cellbits, wordoff, rowoff, x - 1, y, z) - vbase;
-                const uint32_t v2 = vertex_id(d, cellbits, wordoff, rowoff, x, y - 1, z) - vbase;
-                const uint32_t v3 = vertex_id(d, cellbits, wordoff, rowoff, x, y, z) - vbase;
-                if (neg) { t[0] = v0; t[1] = v2; t[2] = v1; t[3] = v1; t[4] = v2; t[5] = v3; }
-                else     { t[0] = v0; t[1] = v1; t[2] = v2; t[3] = v1; t[4] = v3; t[5] = v2; }
-                if (6 * q + 6 <= icap)
-                    for (int k = 0; k < 6; ++k) CG_AT(idx, 6 * q + k, icap) = t[k];
-                ++q;
-            }
-        }
-    }
+    for (uint32_t w = 0; w < d.Wc; ++w)
+        q = quad_emit_word(edge_words(sgn, d, x, y, w), d, dists, cellbits, wordoff, rowoff, vbase,
+                           q, idx, icap, x, y, w);
 }
 
 }  // namespace cg
