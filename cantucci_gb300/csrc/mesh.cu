@@ -68,15 +68,47 @@ __global__ void __launch_bounds__(256) k_sign_words(const float* __restrict__ di
     }
 }
 
-// Surface cells of every cell row; one thread per row (x, y).
+// The row kernels below give a cell row's Wc words (res <= 1024, so Wc is a
+// power of two <= 32) to Wc lanes, 32 / Wc rows per warp: each lane streams
+// its word, and a scan over the row's lanes gives what a walk along the row
+// would (running counts, row totals).  The loop bound is warp-uniform, so
+// every lane reaches every shuffle.
+struct RowLanes {
+    uint32_t L, per_warp, sub, lane_row, warp, nwarps;
+    __device__ RowLanes(const MeshDims& d) {
+        const uint32_t lane = threadIdx.x & 31;
+        L = d.Wc;
+        per_warp = 32 / L;
+        sub = lane % L;
+        lane_row = lane / L;
+        warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        nwarps = (gridDim.x * blockDim.x) >> 5;
+    }
+};
+
+static uint64_t row_lanes(const MeshDims& d) { return (uint64_t)d.res * d.res * d.Wc; }
+
+// Surface cells of every cell row (x, y), with each word's running count
+// and the row's total.
 __global__ void __launch_bounds__(256) k_cells(const uint32_t* __restrict__ sgn, MeshDims d,
                                                uint32_t* __restrict__ cellbits,
                                                uint32_t* __restrict__ wordoff,
                                                uint32_t* __restrict__ rowcnt) {
     const uint32_t rows = d.res * d.res;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-         r += gridDim.x * blockDim.x)
-        CG_AT(rowcnt, r, rows) = cells_row(sgn, d, r, cellbits, wordoff);
+    const uint64_t nc = (uint64_t)rows * d.Wc;
+    const RowLanes g(d);
+    for (uint32_t r0 = g.warp * g.per_warp; r0 < rows; r0 += g.nwarps * g.per_warp) {
+        const uint32_t r = r0 + g.lane_row;
+        const bool ok = r < rows;
+        const uint32_t surf = ok ? cells_word(sgn, d, r, g.sub) : 0u;
+        const uint32_t cnt = __popc(surf);
+        const uint32_t inc = group_inclusive_scan(cnt, g.sub, g.L);
+        if (ok) {
+            CG_AT(cellbits, r * d.Wc + g.sub, nc) = surf;
+            CG_AT(wordoff, r * d.Wc + g.sub, nc) = inc - cnt;
+            if (g.sub == g.L - 1) CG_AT(rowcnt, r, rows) = inc;
+        }
+    }
 }
 
 // Cell index of every vertex, in vertex-id order.
@@ -85,15 +117,76 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
                                                      const uint32_t* __restrict__ rowoff,
                                                      uint32_t* __restrict__ cellidx) {
     const uint32_t rows = d.res * d.res;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-         r += gridDim.x * blockDim.x)
+    const uint64_t nc = (uint64_t)rows * d.Wc;
 #ifdef CG_CHECKED
-        vertex_list_row(d, r, cellbits, wordoff, CG_AT(rowoff, r, rows), (uint64_t)rows * d.res,
-                        cellidx, nullptr, 0);
-#else
-        vertex_list_row(d, r, cellbits, wordoff, rowoff[r], ~0ull, cellidx, nullptr, 0);
+    const uint64_t cap = (uint64_t)rows * d.res;
 #endif
+    const RowLanes g(d);
+    for (uint32_t r0 = g.warp * g.per_warp; r0 < rows; r0 += g.nwarps * g.per_warp) {
+        const uint32_t r = r0 + g.lane_row;
+        if (r >= rows) continue;
+        uint32_t bits = CG_AT(cellbits, r * d.Wc + g.sub, nc);
+        uint32_t v = CG_AT(rowoff, r, rows) + CG_AT(wordoff, r * d.Wc + g.sub, nc);
+        while (bits) {
+            const uint32_t b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            CG_AT(cellidx, v, cap) = r * d.res + g.sub * 32 + b;
+            ++v;
+        }
+    }
 }
+
+// Small spans (at most COMPACT_ROWS cell rows: res <= 64, cantucci's leaf
+// size) in one CTA: the surface cells and quad counts of every row, both
+// exclusive scans, the vertex list and the two totals -- what k_cells, two
+// three-launch scans, k_vertex_list and k_quad_count do on larger spans,
+// with the same outputs, in one launch.
+constexpr uint32_t COMPACT_THREADS = 1024, COMPACT_ROWS_PER_THREAD = 4;
+constexpr uint32_t COMPACT_ROWS = COMPACT_THREADS * COMPACT_ROWS_PER_THREAD;
+
+__global__ void __launch_bounds__(COMPACT_THREADS) k_compact_small(
+    const uint32_t* __restrict__ sgn, MeshDims d, uint32_t* __restrict__ cellbits,
+    uint32_t* __restrict__ wordoff, uint32_t* __restrict__ rowoff,
+    uint32_t* __restrict__ quadoff, uint32_t* __restrict__ cellidx,
+    MeshCounters* __restrict__ counters) {
+    __shared__ uint32_t ws[33];
+    const uint32_t rows = d.res * d.res;
+    const uint32_t r0 = threadIdx.x * COMPACT_ROWS_PER_THREAD;
+    uint32_t vc[COMPACT_ROWS_PER_THREAD], qc[COMPACT_ROWS_PER_THREAD], vs = 0, qs = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < COMPACT_ROWS_PER_THREAD; ++k) {
+        const uint32_t r = r0 + k;
+        vc[k] = r < rows ? cells_row(sgn, d, r, cellbits, wordoff) : 0u;
+        qc[k] = r < rows ? quad_count_row(sgn, d, r) : 0u;
+        vs += vc[k];
+        qs += qc[k];
+    }
+    uint32_t vtot, qtot;
+    uint32_t voff = block_exclusive_scan(vs, ws, vtot);
+    uint32_t qoff = block_exclusive_scan(qs, ws, qtot);
+#pragma unroll
+    for (uint32_t k = 0; k < COMPACT_ROWS_PER_THREAD; ++k) {
+        const uint32_t r = r0 + k;
+        if (r < rows) {
+            CG_AT(rowoff, r, rows) = voff;
+            CG_AT(quadoff, r, rows) = qoff;
+#ifdef CG_CHECKED
+            vertex_list_row(d, r, cellbits, wordoff, voff, (uint64_t)rows * d.res, cellidx,
+                            nullptr, 0);
+#else
+            vertex_list_row(d, r, cellbits, wordoff, voff, ~0ull, cellidx, nullptr, 0);
+#endif
+        }
+        voff += vc[k];
+        qoff += qc[k];
+    }
+    if (threadIdx.x == 0) {
+        counters->vertices = vtot;
+        counters->quads = qtot;
+    }
+}
+
+static bool compact_in_one_block(const MeshDims& d) { return d.res * d.res <= COMPACT_ROWS; }
 
 // One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
 // vertices and stores them through shared memory as 16-byte chunks (32
@@ -229,17 +322,18 @@ __global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, M
 __global__ void __launch_bounds__(256) k_quad_count(const uint32_t* __restrict__ sgn, MeshDims d,
                                                     uint32_t* __restrict__ quadcnt) {
     const uint32_t rows = d.res * d.res;
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
-         r += gridDim.x * blockDim.x)
-        CG_AT(quadcnt, r, rows) = quad_count_row(sgn, d, r);
+    const RowLanes g(d);
+    for (uint32_t r0 = g.warp * g.per_warp; r0 < rows; r0 += g.nwarps * g.per_warp) {
+        const uint32_t r = r0 + g.lane_row;
+        const bool ok = r < rows;
+        EdgeWords e = {0u, 0u, 0u};
+        if (ok) e = edge_words(sgn, d, r / d.res, r % d.res, g.sub);
+        const uint32_t inc =
+            group_inclusive_scan(__popc(e.ex) + __popc(e.ey) + __popc(e.ez), g.sub, g.L);
+        if (ok && g.sub == g.L - 1) CG_AT(quadcnt, r, rows) = inc;
+    }
 }
 
-// Warp-cooperative quad emission: a row's Wc sign words (res <= 1024, so Wc
-// is a power of two <= 32) go to Wc lanes, 32 / Wc rows per warp.  Each lane
-// counts its word's quads, a segmented scan over the row's lanes gives the
-// word's first quad, and the lane writes them: the same list as one thread
-// per row walking the words in order, with the row's quads spread over its
-// lanes and their stores side by side.
 __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ sgn, MeshDims d,
                                                    const float* __restrict__ dists,
                                                    const uint32_t* __restrict__ cellbits,
@@ -248,26 +342,10 @@ __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ 
                                                    const uint32_t* __restrict__ quadoff,
                                                    uint32_t* __restrict__ idx, uint64_t icap) {
     const uint32_t rows = d.res * d.res;
-    const uint32_t L = d.Wc, per_warp = 32 / L;
-    const uint32_t lane = threadIdx.x & 31, sub = lane % L;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t r0 = warp * per_warp; r0 < rows; r0 += nwarps * per_warp) {
-        const uint32_t r = r0 + lane / L;
-        const bool ok = r < rows;
-        const uint32_t x = ok ? r / d.res : 0u, y = ok ? r % d.res : 0u;
-        EdgeWords e = {0u, 0u, 0u};
-        if (ok) e = edge_words(sgn, d, x, y, sub);
-        const uint32_t cnt = __popc(e.ex) + __popc(e.ey) + __popc(e.ez);
-        uint32_t inc = cnt;
-        for (uint32_t o = 1; o < L; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, L);
-            if (sub >= o) inc += v;
-        }
-        if (ok && cnt)
-            quad_emit_word(e, d, dists, cellbits, wordoff, rowoff, 0u,
-                           (uint64_t)CG_AT(quadoff, r, rows) + (inc - cnt), idx, icap, x, y, sub);
-    }
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x)
+        quad_emit_row(sgn, d, dists, cellbits, wordoff, rowoff, 0u, CG_AT(quadoff, r, rows), idx,
+                      icap, r);
 }
 
 // Copy of the first n words of src (n <= src_cap) to dst (n <= dst_cap),
@@ -488,7 +566,8 @@ static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const Mesh
     return CG_OK;
 }
 
-// Surface cells, their scan and the vertex list (step 2 up to placement).
+// Surface cells, their scan and the vertex list (step 2 up to placement);
+// on small spans also the quad counts and their scan (k_compact_small).
 static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t st,
                               bool signs_ready) {
     const uint32_t rows = d.res * d.res;
@@ -499,23 +578,31 @@ static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t
         k_sign_words<<<G, B, 0, st>>>(w.dists, d.n, d.W, w.sgn);
         CG_CHECK_LAUNCH("k_sign_words");
     }
+    if (compact_in_one_block(d)) {
+        k_compact_small<<<1, COMPACT_THREADS, 0, st>>>(w.sgn, d, w.cellbits, w.wordoff, w.rowoff,
+                                                       w.quadoff, w.cellidx, w.counters);
+        CG_CHECK_LAUNCH("k_compact_small");
+        return CG_OK;
+    }
     {
-        const unsigned B = 256, G = grid_for(rows, B, 8);
+        const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
         k_cells<<<G, B, 0, st>>>(w.sgn, d, w.cellbits, w.wordoff, w.rowcnt);
         CG_CHECK_LAUNCH("k_cells");
     }
     CG_TRY(launch_exclusive_scan(w.rowcnt, w.rowoff, rows, w.scratch, &w.counters->vertices, st));
     {
-        const unsigned B = 256, G = grid_for(rows, B, 8);
+        const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
         k_vertex_list<<<G, B, 0, st>>>(d, w.cellbits, w.wordoff, w.rowoff, w.cellidx);
         CG_CHECK_LAUNCH("k_vertex_list");
     }
     return CG_OK;
 }
 
+// Quad counts and their scan (done by launch_cells on small spans).
 static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStream_t st) {
+    if (compact_in_one_block(d)) return CG_OK;
     const uint32_t rows = d.res * d.res;
-    const unsigned B = 256, G = grid_for(rows, B, 8);
+    const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
     k_quad_count<<<G, B, 0, st>>>(w.sgn, d, w.quadcnt);
     CG_CHECK_LAUNCH("k_quad_count");
     CG_TRY(launch_exclusive_scan(w.quadcnt, w.quadoff, rows, w.scratch, &w.counters->quads, st));
@@ -524,8 +611,8 @@ static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStr
 
 static cg_status launch_quad_emit(const MeshDims& d, const MeshWork& w, uint32_t* idx,
                                   uint64_t icap, cudaStream_t st) {
-    const uint64_t lanes = (uint64_t)d.res * d.res * d.Wc;
-    const unsigned B = 256, G = grid_for(lanes, B, 8);
+    const uint32_t rows = d.res * d.res;
+    const unsigned B = 256, G = grid_for(rows, B, 8);
     k_quad_emit<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff, w.quadoff,
                                  idx, icap);
     CG_CHECK_LAUNCH("k_quad_emit");

@@ -36,28 +36,45 @@ __device__ __forceinline__ uint32_t sign_hi(const uint32_t* __restrict__ sgn, co
     return (lo >> 1) | (nx << 31);
 }
 
-// Surface cells of cell row r = (x, y) (buffer.rs:116-147): a cell crosses
-// iff the sign bits of its 8 corners are not all equal.  Returns the count.
+// Surface cells of word w of cell row r = (x, y) (buffer.rs:116-147): a
+// cell crosses iff the sign bits of its 8 corners are not all equal.
+__device__ __forceinline__ uint32_t cells_word(const uint32_t* __restrict__ sgn, const MeshDims& d,
+                                               uint32_t r, uint32_t w) {
+    const uint32_t x = r / d.res, y = r % d.res;
+    const uint32_t r00 = x * d.n + y, r01 = r00 + 1, r10 = r00 + d.n, r11 = r10 + 1;
+    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    const uint32_t a0 = CG_AT(sgn, r00 * d.W + w, ns), a1 = CG_AT(sgn, r01 * d.W + w, ns);
+    const uint32_t a2 = CG_AT(sgn, r10 * d.W + w, ns), a3 = CG_AT(sgn, r11 * d.W + w, ns);
+    const uint32_t b0 = sign_hi(sgn, d, r00, w), b1 = sign_hi(sgn, d, r01, w);
+    const uint32_t b2 = sign_hi(sgn, d, r10, w), b3 = sign_hi(sgn, d, r11, w);
+    const uint32_t all1 = a0 & a1 & a2 & a3 & b0 & b1 & b2 & b3;
+    const uint32_t any1 = a0 | a1 | a2 | a3 | b0 | b1 | b2 | b3;
+    return any1 & ~all1 & valid_mask(d.res, w);
+}
+
+// The surface cells of cell row r, word by word, with each word's running
+// count before it; returns the row's count.
 __device__ __forceinline__ uint32_t cells_row(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                               uint32_t r, uint32_t* __restrict__ cellbits,
                                               uint32_t* __restrict__ wordoff) {
-    const uint32_t x = r / d.res, y = r % d.res;
-    const uint32_t r00 = x * d.n + y, r01 = r00 + 1, r10 = r00 + d.n, r11 = r10 + 1;
     uint32_t run = 0;
     for (uint32_t w = 0; w < d.Wc; ++w) {
-        const uint64_t ns = (uint64_t)d.n * d.n * d.W;
-        const uint32_t a0 = CG_AT(sgn, r00 * d.W + w, ns), a1 = CG_AT(sgn, r01 * d.W + w, ns);
-        const uint32_t a2 = CG_AT(sgn, r10 * d.W + w, ns), a3 = CG_AT(sgn, r11 * d.W + w, ns);
-        const uint32_t b0 = sign_hi(sgn, d, r00, w), b1 = sign_hi(sgn, d, r01, w);
-        const uint32_t b2 = sign_hi(sgn, d, r10, w), b3 = sign_hi(sgn, d, r11, w);
-        const uint32_t all1 = a0 & a1 & a2 & a3 & b0 & b1 & b2 & b3;
-        const uint32_t any1 = a0 | a1 | a2 | a3 | b0 | b1 | b2 | b3;
-        const uint32_t surf = any1 & ~all1 & valid_mask(d.res, w);
+        const uint32_t surf = cells_word(sgn, d, r, w);
         CG_AT(cellbits, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc) = surf;
         CG_AT(wordoff, r * d.Wc + w, (uint64_t)d.res * d.res * d.Wc) = run;
         run += __popc(surf);
     }
     return run;
+}
+
+// Inclusive scan of v over aligned groups of L lanes (L a power of two <=
+// 32; sub = lane % L); every lane of the warp calls it.
+__device__ __forceinline__ uint32_t group_inclusive_scan(uint32_t v, uint32_t sub, uint32_t L) {
+    for (uint32_t o = 1; o < L; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, v, o, L);
+        if (sub >= o) v += t;
+    }
+    return v;
 }
 
 // Cell index (within its span) of every vertex of cell row r, written at the

@@ -16,37 +16,6 @@ constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
-// Exclusive scan of one value per thread across the CTA; returns the CTA total.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums,
-                                                         uint32_t& total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-        uint32_t w = lane < nw ? warp_sums[lane] : 0;
-        uint32_t wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-            if (lane >= o) wi += t;
-        }
-        if (lane < nw) warp_sums[lane] = wi - w;  // exclusive warp offsets
-        if (lane == nw - 1) warp_sums[32] = wi;   // CTA total
-    }
-    __syncthreads();
-    const uint32_t res = warp_sums[warp] + inc - v;
-    total = warp_sums[32];
-    __syncthreads();
-    return res;
-}
-
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in,
                                                               uint32_t n,
                                                               uint32_t* __restrict__ tile_sums) {
