@@ -186,7 +186,12 @@ __global__ void __launch_bounds__(COMPACT_THREADS) k_compact_small(
     }
 }
 
-static bool compact_in_one_block(const MeshDims& d) { return d.res * d.res <= COMPACT_ROWS; }
+// cg_set_option("small_compaction", 0/1): whether small spans take it.
+static std::atomic<int> g_small_compaction{1};
+
+static bool compact_in_one_block(const MeshDims& d) {
+    return g_small_compaction.load() && d.res * d.res <= COMPACT_ROWS;
+}
 
 // One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
 // vertices and stores them through shared memory as 16-byte chunks (32
@@ -319,19 +324,14 @@ __global__ void __launch_bounds__(128) k_edge_data(ShapeDev s, PlaceParams pp, M
     }
 }
 
+// Quads of every corner row, one thread per row: the per-lane version of
+// the kernels above measured slower here (22 against 17 us at res 512).
 __global__ void __launch_bounds__(256) k_quad_count(const uint32_t* __restrict__ sgn, MeshDims d,
                                                     uint32_t* __restrict__ quadcnt) {
     const uint32_t rows = d.res * d.res;
-    const RowLanes g(d);
-    for (uint32_t r0 = g.warp * g.per_warp; r0 < rows; r0 += g.nwarps * g.per_warp) {
-        const uint32_t r = r0 + g.lane_row;
-        const bool ok = r < rows;
-        EdgeWords e = {0u, 0u, 0u};
-        if (ok) e = edge_words(sgn, d, r / d.res, r % d.res, g.sub);
-        const uint32_t inc =
-            group_inclusive_scan(__popc(e.ex) + __popc(e.ey) + __popc(e.ez), g.sub, g.L);
-        if (ok && g.sub == g.L - 1) CG_AT(quadcnt, r, rows) = inc;
-    }
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+         r += gridDim.x * blockDim.x)
+        CG_AT(quadcnt, r, rows) = quad_count_row(sgn, d, r);
 }
 
 __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ sgn, MeshDims d,
@@ -412,6 +412,10 @@ static std::atomic<uint32_t> g_place_blocks_per_sm{128};
 uint32_t place_blocks_per_sm() { return g_place_blocks_per_sm.load(); }
 
 int set_place_option(const char* name, int64_t v) {
+    if (!strcmp(name, "small_compaction") && (v == 0 || v == 1)) {
+        g_small_compaction.store((int)v);
+        return 1;
+    }
     if (strcmp(name, "place_blocks_per_sm") || v < 1 || v > 1024) return 0;
     g_place_blocks_per_sm.store((uint32_t)v);
     return 1;
@@ -602,7 +606,7 @@ static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t
 static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStream_t st) {
     if (compact_in_one_block(d)) return CG_OK;
     const uint32_t rows = d.res * d.res;
-    const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
+    const unsigned B = 256, G = grid_for(rows, B, 8);
     k_quad_count<<<G, B, 0, st>>>(w.sgn, d, w.quadcnt);
     CG_CHECK_LAUNCH("k_quad_count");
     CG_TRY(launch_exclusive_scan(w.quadcnt, w.quadoff, rows, w.scratch, &w.counters->quads, st));
