@@ -136,63 +136,6 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
     }
 }
 
-// Small spans (at most COMPACT_ROWS cell rows: res <= 64, cantucci's leaf
-// size) in one CTA: the surface cells and quad counts of every row, both
-// exclusive scans, the vertex list and the two totals -- what k_cells, two
-// three-launch scans, k_vertex_list and k_quad_count do on larger spans,
-// with the same outputs, in one launch.
-constexpr uint32_t COMPACT_THREADS = 1024, COMPACT_ROWS_PER_THREAD = 4;
-constexpr uint32_t COMPACT_ROWS = COMPACT_THREADS * COMPACT_ROWS_PER_THREAD;
-
-__global__ void __launch_bounds__(COMPACT_THREADS) k_compact_small(
-    const uint32_t* __restrict__ sgn, MeshDims d, uint32_t* __restrict__ cellbits,
-    uint32_t* __restrict__ wordoff, uint32_t* __restrict__ rowoff,
-    uint32_t* __restrict__ quadoff, uint32_t* __restrict__ cellidx,
-    MeshCounters* __restrict__ counters) {
-    __shared__ uint32_t ws[33];
-    const uint32_t rows = d.res * d.res;
-    const uint32_t r0 = threadIdx.x * COMPACT_ROWS_PER_THREAD;
-    uint32_t vc[COMPACT_ROWS_PER_THREAD], qc[COMPACT_ROWS_PER_THREAD], vs = 0, qs = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < COMPACT_ROWS_PER_THREAD; ++k) {
-        const uint32_t r = r0 + k;
-        vc[k] = r < rows ? cells_row(sgn, d, r, cellbits, wordoff) : 0u;
-        qc[k] = r < rows ? quad_count_row(sgn, d, r) : 0u;
-        vs += vc[k];
-        qs += qc[k];
-    }
-    uint32_t vtot, qtot;
-    uint32_t voff = block_exclusive_scan(vs, ws, vtot);
-    uint32_t qoff = block_exclusive_scan(qs, ws, qtot);
-#pragma unroll
-    for (uint32_t k = 0; k < COMPACT_ROWS_PER_THREAD; ++k) {
-        const uint32_t r = r0 + k;
-        if (r < rows) {
-            CG_AT(rowoff, r, rows) = voff;
-            CG_AT(quadoff, r, rows) = qoff;
-#ifdef CG_CHECKED
-            vertex_list_row(d, r, cellbits, wordoff, voff, (uint64_t)rows * d.res, cellidx,
-                            nullptr, 0);
-#else
-            vertex_list_row(d, r, cellbits, wordoff, voff, ~0ull, cellidx, nullptr, 0);
-#endif
-        }
-        voff += vc[k];
-        qoff += qc[k];
-    }
-    if (threadIdx.x == 0) {
-        counters->vertices = vtot;
-        counters->quads = qtot;
-    }
-}
-
-// cg_set_option("small_compaction", 0/1): whether small spans take it.
-static std::atomic<int> g_small_compaction{1};
-
-static bool compact_in_one_block(const MeshDims& d) {
-    return g_small_compaction.load() && d.res * d.res <= COMPACT_ROWS;
-}
-
 // One vertex per thread (buffer.rs:149-274).  A warp places 32 consecutive
 // vertices and stores them through shared memory as 16-byte chunks (32
 // vertices = 896 bytes = 56 float4), so the stores are coalesced whether
@@ -411,11 +354,17 @@ static std::atomic<uint32_t> g_place_blocks_per_sm{128};
 
 uint32_t place_blocks_per_sm() { return g_place_blocks_per_sm.load(); }
 
+// The placement grid: place_blocks_per_sm per SM, but no more blocks than
+// the span's res^3 cells (the most vertices it can have) fill.  Blocks past
+// the vertex count exit at once, yet each still has to be scheduled: on a
+// res-64 span the full grid is 19,456 blocks for some 150 with work.
+static unsigned place_grid(const MeshDims& d, unsigned block) {
+    const uint64_t cap = (uint64_t)sm_count() * g_place_blocks_per_sm.load();
+    const uint64_t need = ((uint64_t)d.res * d.res * d.res + block - 1) / block;
+    return (unsigned)(need < cap ? need : cap);
+}
+
 int set_place_option(const char* name, int64_t v) {
-    if (!strcmp(name, "small_compaction") && (v == 0 || v == 1)) {
-        g_small_compaction.store((int)v);
-        return 1;
-    }
     if (strcmp(name, "place_blocks_per_sm") || v < 1 || v > 1024) return 0;
     g_place_blocks_per_sm.store((uint32_t)v);
     return 1;
@@ -426,7 +375,7 @@ static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const Me
                               const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                               cudaStream_t st, const PlaceOptions& opt, const EdgeTable& et) {
     const unsigned B = 128;
-    const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
+    const unsigned G = place_grid(d, B);
     if (opt.qef)
         k_place<M, AN, false, true><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                      verts, vcap, 0, et, opt.pp_dev);
@@ -534,7 +483,7 @@ static void launch_place_plain(const ShapeDev& s, const PlaceParams& pp, const M
                                const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                cudaStream_t st, const PlaceParams* pp_dev) {
     const unsigned B = 128;
-    const unsigned G = (unsigned)sm_count() * g_place_blocks_per_sm.load();
+    const unsigned G = place_grid(d, B);
     k_place<M, false, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                      verts, vcap, 0, EdgeTable{}, pp_dev);
 }
@@ -570,8 +519,7 @@ static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const Mesh
     return CG_OK;
 }
 
-// Surface cells, their scan and the vertex list (step 2 up to placement);
-// on small spans also the quad counts and their scan (k_compact_small).
+// Surface cells, their scan and the vertex list (step 2 up to placement).
 static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t st,
                               bool signs_ready) {
     const uint32_t rows = d.res * d.res;
@@ -581,12 +529,6 @@ static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t
         const unsigned B = 256, G = grid_for(warps * 32, B, 8);
         k_sign_words<<<G, B, 0, st>>>(w.dists, d.n, d.W, w.sgn);
         CG_CHECK_LAUNCH("k_sign_words");
-    }
-    if (compact_in_one_block(d)) {
-        k_compact_small<<<1, COMPACT_THREADS, 0, st>>>(w.sgn, d, w.cellbits, w.wordoff, w.rowoff,
-                                                       w.quadoff, w.cellidx, w.counters);
-        CG_CHECK_LAUNCH("k_compact_small");
-        return CG_OK;
     }
     {
         const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
@@ -602,9 +544,7 @@ static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t
     return CG_OK;
 }
 
-// Quad counts and their scan (done by launch_cells on small spans).
 static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStream_t st) {
-    if (compact_in_one_block(d)) return CG_OK;
     const uint32_t rows = d.res * d.res;
     const unsigned B = 256, G = grid_for(rows, B, 8);
     k_quad_count<<<G, B, 0, st>>>(w.sgn, d, w.quadcnt);

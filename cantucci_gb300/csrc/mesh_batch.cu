@@ -413,7 +413,13 @@ cg_status launch_batch_place(cg_batch* b, const ShapeDev& s, cg_vertex* vertices
     // Eight waves of blocks rather than one resident wave, so that blocks
     // finish throughout the launch (as k_place: measured 10.19 -> 10.02 ms
     // on the 4096-span batch together with the side stream's priority).
-    const unsigned G = resident_grid(k_batch_place<M, AN>, B) * 8;
+    // No more blocks than the spans' cells (the most vertices they can have)
+    // fill: a small batch would otherwise schedule thousands of empty blocks.
+    uint64_t cells = 0;
+    for (uint32_t r : b->res) cells += (uint64_t)r * r * r;
+    const uint64_t need = (cells + B - 1) / B;
+    const uint64_t full = (uint64_t)resident_grid(k_batch_place<M, AN>, B) * 8;
+    const unsigned G = (unsigned)(need < full ? (need ? need : 1) : full);
     k_batch_place<M, AN><<<G, B, 0, st>>>(s, b->jobs, b->dists, b->cellidx, b->celljob, b->tot,
                                       vertices, vertex_cap);
     CG_CHECK_LAUNCH("k_batch_place");
