@@ -618,7 +618,7 @@ def extra_fp64_check(dev, res=RES, stride=67):
 def extra_small_span(dev, reps=50):
     """Config 1: the 65^3-corner span (res 64, the reference's leaf
     resolution) meshed alone, device outputs and pinned host outputs: a
-    latency-bound call (12 kernels on 274,625 corners)."""
+    latency-bound call (8 kernels on 274,625 corners: the scans fit one tile)."""
     import numpy as np
     import torch
     import cantucci_gb300 as cg

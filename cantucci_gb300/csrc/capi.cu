@@ -263,7 +263,7 @@ cg_status enqueue_mesh(cg_mesher* m, const ShapeDev& s, const SpanSetup& su, con
 }
 
 // Meshes into the graph kept for this mesher, capturing it first if the key
-// changed.  Only up to kGraphMaxRes: there the 12 launches cost about as
+// changed.  Only up to kGraphMaxRes: there the launches cost about as
 // much as the work, while in a large mesh they are negligible and a
 // replayed graph loses the side stream's priority (its quads then end 0.2 ms
 // after the placement on the 513^3 span instead of under it).  Returns false

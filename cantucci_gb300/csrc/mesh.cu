@@ -89,11 +89,17 @@ struct RowLanes {
 static uint64_t row_lanes(const MeshDims& d) { return (uint64_t)d.res * d.res * d.Wc; }
 
 // Surface cells of every cell row (x, y), with each word's running count
-// and the row's total.
+// and the row's total.  Also clears the counters the later kernels
+// accumulate into (the totals come from the scans), in place of a memset.
 __global__ void __launch_bounds__(256) k_cells(const uint32_t* __restrict__ sgn, MeshDims d,
                                                uint32_t* __restrict__ cellbits,
                                                uint32_t* __restrict__ wordoff,
-                                               uint32_t* __restrict__ rowcnt) {
+                                               uint32_t* __restrict__ rowcnt,
+                                               MeshCounters* __restrict__ cnt) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        cnt->status = 0;
+        cnt->edges = 0;
+    }
     const uint32_t rows = d.res * d.res;
     const uint64_t nc = (uint64_t)rows * d.Wc;
     const RowLanes g(d);
@@ -523,7 +529,6 @@ static cg_status launch_place(const ShapeDev& s, const SpanSetup& su, const Mesh
 static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t st,
                               bool signs_ready) {
     const uint32_t rows = d.res * d.res;
-    CG_CUDA(cudaMemsetAsync(w.counters, 0, sizeof(MeshCounters), st));
     if (!signs_ready) {
         const uint64_t warps = (uint64_t)d.n * d.n * d.W;
         const unsigned B = 256, G = grid_for(warps * 32, B, 8);
@@ -532,7 +537,7 @@ static cg_status launch_cells(const MeshDims& d, const MeshWork& w, cudaStream_t
     }
     {
         const unsigned B = 256, G = grid_for(row_lanes(d), B, 8);
-        k_cells<<<G, B, 0, st>>>(w.sgn, d, w.cellbits, w.wordoff, w.rowcnt);
+        k_cells<<<G, B, 0, st>>>(w.sgn, d, w.cellbits, w.wordoff, w.rowcnt, w.counters);
         CG_CHECK_LAUNCH("k_cells");
     }
     CG_TRY(launch_exclusive_scan(w.rowcnt, w.rowoff, rows, w.scratch, &w.counters->vertices, st));

@@ -3,8 +3,9 @@
 // reference's cube() order (src/util/iter.rs:31-51).
 //
 // Three launches: per-tile sums, one-CTA scan of the tile sums, per-tile scan
-// plus offset.  Tiles are 4096 counts (1024 threads x 4), so one top-level
-// CTA covers 4096 tiles = 16M counts, enough for res^2 rows at res <= 1024.
+// plus offset; one launch when the counts fit one tile.  Tiles are 4096
+// counts (1024 threads x 4), so one top-level CTA covers 4096 tiles = 16M
+// counts, enough for res^2 rows at res <= 1024.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -73,6 +74,28 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
     }
 }
 
+// n <= SCAN_TILE (rows of a span up to res 64): the whole scan in one CTA.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile(const uint32_t* __restrict__ in,
+                                                            uint32_t n, uint32_t* __restrict__ out,
+                                                            uint32_t* __restrict__ total) {
+    __shared__ uint32_t ws[33];
+    const uint32_t base = threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS], s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = (base + k < n) ? CG_AT(in, base + k, n) : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t off = block_exclusive_scan(s, ws, tot);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < n) CG_AT(out, base + k, n) = off;
+        off += v[k];
+    }
+    if (threadIdx.x == 0) *total = tot;
+}
+
 size_t scan_scratch_words(uint32_t n) {
     return (n + SCAN_TILE - 1) / SCAN_TILE + 1;
 }
@@ -87,6 +110,11 @@ cg_status launch_exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, u
     }
     if (n == 0) {
         CG_CUDA(cudaMemsetAsync(total, 0, sizeof(uint32_t), st));
+        return CG_OK;
+    }
+    if (ntiles == 1) {
+        k_scan_tile<<<1, SCAN_THREADS, 0, st>>>(in, n, out, total);
+        CG_CHECK_LAUNCH("k_scan_tile");
         return CG_OK;
     }
     k_scan_reduce<<<ntiles, SCAN_THREADS, 0, st>>>(in, n, scratch);
