@@ -205,8 +205,10 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic", "config": {"workload": WORKLOAD, "res": RES},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": text + " (the Rust reference is x86-only and not buildable "
-                                          "here; this is its C restatement)"},
+                         "sample": text + " (the Rust reference is x86-64 only: its Vec3 "
+                                          "uses SSE4.1; this is its C restatement, "
+                                          "bit-identical to a C++ translation of its own "
+                                          "source on x86-64)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
