@@ -11,9 +11,13 @@
 // branchy) and the two data-parallel parts go to the GPU: the focus rays are
 // one k_march launch, and all of an update's jobs are one batched mesher run
 // (mesh_batch.cu) on the driver's stream, left in flight until a later
-// update finds its event complete.  A run writes one vertex and one index
-// buffer (a "generation"); ready leaves point into it, and a generation is
-// freed when no leaf points into it any more.
+// update finds its event complete.  Like the reference's thread pool, which
+// takes new jobs while older ones run, an update starts a run for the
+// leaves that became empty even while earlier runs are in flight (up to
+// kMaxRuns queued on the stream; they finish and are collected in launch
+// order).  A run writes one vertex and one index buffer (a "generation");
+// ready leaves point into it, and a generation is freed when no leaf points
+// into it any more.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -30,6 +34,7 @@ namespace {
 constexpr uint32_t kFocusPoints = 5;        // FOCUS_POINTS (mod.rs:88)
 constexpr uint32_t kFocusSteps = 100;       // MAX_ITERS of get_focii (mod.rs:207)
 constexpr float kFocusEpsilon = 0.000001f;  // EPSILON of get_focii (mod.rs:206)
+constexpr uint32_t kMaxRuns = 4;            // batched runs queued at once
 
 struct V3 {
     float x, y, z;
@@ -80,6 +85,21 @@ struct Generation {
     uint32_t refs = 0;
 };
 
+// One batched mesher run and what it needs until it is collected.
+struct Run {
+    cg_batch* batch = nullptr;
+    cudaEvent_t done = nullptr;
+    bool inflight = false;
+    int32_t gen = -1;
+    uint64_t vcap = 0, icap = 0;
+    std::vector<cg_span_job> jobs;
+    cg_job_mesh* d_results = nullptr;  // device, batch capacity
+    cg_job_mesh* h_results = nullptr;  // pinned
+    uint32_t results_cap = 0;
+    uint32_t* d_totals = nullptr;      // device, 4 words
+    uint32_t* h_totals = nullptr;      // pinned
+};
+
 }  // namespace
 }  // namespace cg
 
@@ -92,21 +112,12 @@ struct cg_shape_mesh {
     uint32_t res = 64;
     cudaStream_t stream = nullptr;  // mesh jobs
     cudaStream_t fstream = nullptr; // focus rays (not queued behind the jobs)
-    cudaEvent_t done = nullptr;
     std::vector<Node> nodes;
     std::vector<Generation> gens;
-    cg_batch* batch = nullptr;
     uint32_t normals = CG_NORMALS_FD, numerics = CG_NUMERICS_EXACT;
-    // the run in flight
-    bool inflight = false;
-    int32_t run_gen = -1;
-    uint64_t run_vcap = 0, run_icap = 0;
-    std::vector<cg_span_job> run_jobs;
-    cg_job_mesh* d_results = nullptr;  // device, batch capacity
-    uint32_t* d_totals = nullptr;      // device, 4 words
-    cg_job_mesh* h_results = nullptr;  // pinned
-    uint32_t* h_totals = nullptr;      // pinned
-    uint32_t results_cap = 0;
+    // run slots; `queue` holds the ones in flight, oldest first
+    Run runs[kMaxRuns];
+    std::vector<uint32_t> queue;
     // focus rays
     float* d_rays = nullptr;  // org | dir | hits, 3 x 3 x F^2 floats
     uint8_t* d_hit = nullptr;
@@ -231,78 +242,95 @@ cg_status focus_rays(const cg_view& v, uint32_t F, float* org, float* dir) {
     return CG_OK;
 }
 
-// Grows the batch to hold `jobs` (a new batch when the job list does not fit).
-cg_status fit_batch(cg_shape_mesh* sm, const std::vector<cg_span_job>& jobs) {
+// Grows the run's batch to hold `jobs` (a new batch when the job list does
+// not fit).
+cg_status fit_batch(cg_shape_mesh* sm, Run& run, const std::vector<cg_span_job>& jobs) {
     const uint32_t n = (uint32_t)jobs.size();
-    if (sm->batch) {
-        const cg_status st = cg_batch_set_jobs(sm->batch, jobs.data(), n);
+    if (run.batch) {
+        const cg_status st = cg_batch_set_jobs(run.batch, jobs.data(), n);
         if (st == CG_OK) return CG_OK;
         if (st != CG_ECAPACITY) return st;
-        cg_batch_destroy(sm->batch);
-        sm->batch = nullptr;
+        cg_batch_destroy(run.batch);
+        run.batch = nullptr;
     }
     // Room for twice as many jobs, so the next updates rarely reallocate.
     std::vector<cg_span_job> padded(jobs);
     while (padded.size() < 2 * jobs.size()) padded.push_back(jobs.back());
     const uint64_t r3 = (uint64_t)sm->res * sm->res * sm->res;
     CG_TRY(cg_batch_create(sm->device, padded.data(), (uint32_t)padded.size(),
-                           r3 * padded.size(), &sm->batch));
-    CG_TRY(cg_batch_set_jobs(sm->batch, jobs.data(), n));
-    if (sm->results_cap < padded.size()) {
-        if (sm->d_results) cudaFree(sm->d_results);
-        if (sm->h_results) cudaFreeHost(sm->h_results);
-        sm->d_results = nullptr;
-        sm->h_results = nullptr;
-        sm->results_cap = 0;
-        CG_CUDA(cudaMalloc(&sm->d_results, sizeof(cg_job_mesh) * padded.size()));
-        CG_CUDA(cudaMallocHost(&sm->h_results, sizeof(cg_job_mesh) * padded.size()));
-        sm->results_cap = (uint32_t)padded.size();
+                           r3 * padded.size(), &run.batch));
+    CG_TRY(cg_batch_set_jobs(run.batch, jobs.data(), n));
+    if (run.results_cap < padded.size()) {
+        if (run.d_results) cudaFree(run.d_results);
+        if (run.h_results) cudaFreeHost(run.h_results);
+        run.d_results = nullptr;
+        run.h_results = nullptr;
+        run.results_cap = 0;
+        CG_CUDA(cudaMalloc(&run.d_results, sizeof(cg_job_mesh) * padded.size()));
+        CG_CUDA(cudaMallocHost(&run.h_results, sizeof(cg_job_mesh) * padded.size()));
+        run.results_cap = (uint32_t)padded.size();
     }
+    if (!run.d_totals) {
+        CG_CUDA(cudaMalloc(&run.d_totals, 4 * sizeof(uint32_t)));
+        CG_CUDA(cudaMallocHost(&run.h_totals, 4 * sizeof(uint32_t)));
+    }
+    if (!run.done) CG_CUDA(cudaEventCreateWithFlags(&run.done, cudaEventDisableTiming));
     return CG_OK;
 }
 
-// Launches the batch into generation `gen` with its current capacities.
-cg_status launch_run(cg_shape_mesh* sm) {
-    Generation& g = sm->gens[sm->run_gen];
-    CG_TRY(cg_batch_set_normals(sm->batch, sm->normals));
-    CG_TRY(cg_batch_set_numerics(sm->batch, sm->numerics));
-    CG_TRY(cg_batch_mesh(sm->batch, &sm->shape, g.verts, sm->run_vcap, g.idx, sm->run_icap,
-                         sm->d_results, sm->d_totals, sm->stream));
-    CG_CUDA(cudaMemcpyAsync(sm->h_results, sm->d_results,
-                            sizeof(cg_job_mesh) * sm->run_jobs.size(), cudaMemcpyDeviceToHost,
-                            sm->stream));
-    CG_CUDA(cudaMemcpyAsync(sm->h_totals, sm->d_totals, 3 * sizeof(uint32_t),
+// Launches the run's batch into its generation with its current capacities.
+cg_status launch_run(cg_shape_mesh* sm, Run& run) {
+    Generation& g = sm->gens[run.gen];
+    CG_TRY(cg_batch_set_normals(run.batch, sm->normals));
+    CG_TRY(cg_batch_set_numerics(run.batch, sm->numerics));
+    CG_TRY(cg_batch_mesh(run.batch, &sm->shape, g.verts, run.vcap, g.idx, run.icap,
+                         run.d_results, run.d_totals, sm->stream));
+    CG_CUDA(cudaMemcpyAsync(run.h_results, run.d_results, sizeof(cg_job_mesh) * run.jobs.size(),
                             cudaMemcpyDeviceToHost, sm->stream));
-    CG_CUDA(cudaEventRecord(sm->done, sm->stream));
+    CG_CUDA(cudaMemcpyAsync(run.h_totals, run.d_totals, 3 * sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, sm->stream));
+    CG_CUDA(cudaEventRecord(run.done, sm->stream));
     return CG_OK;
 }
 
-cg_status alloc_gen_buffers(cg_shape_mesh* sm, Generation& g) {
+cg_status alloc_gen_buffers(cg_shape_mesh* sm, const Run& run, Generation& g) {
     CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&g.verts),
-                            sizeof(cg_vertex) * (sm->run_vcap ? sm->run_vcap : 1), sm->stream));
+                            sizeof(cg_vertex) * (run.vcap ? run.vcap : 1), sm->stream));
     CG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&g.idx),
-                            sizeof(uint32_t) * (sm->run_icap ? sm->run_icap : 1), sm->stream));
+                            sizeof(uint32_t) * (run.icap ? run.icap : 1), sm->stream));
     return CG_OK;
+}
+
+void free_run(Run& run) {
+    if (run.batch) cg_batch_destroy(run.batch);
+    if (run.d_results) cudaFree(run.d_results);
+    if (run.h_results) cudaFreeHost(run.h_results);
+    if (run.d_totals) cudaFree(run.d_totals);
+    if (run.h_totals) cudaFreeHost(run.h_totals);
+    if (run.done) cudaEventDestroy(run.done);
+    run = Run{};
 }
 
 // Collects a finished run: grows and reruns it once if an output overflowed,
-// then hands every job's mesh to the leaf around its span's centre.
-cg_status collect(cg_shape_mesh* sm, uint32_t* collected) {
-    CG_CUDA(cudaEventSynchronize(sm->done));
-    const uint64_t nv = sm->h_totals[0], ni = 6ull * sm->h_totals[1];
-    if (nv > sm->run_vcap || ni > sm->run_icap) {
-        Generation& g = sm->gens[sm->run_gen];
+// then hands every job's mesh to the leaf around its span's centre.  A rerun
+// goes to the back of the stream, so it waits for the runs queued after
+// this one; the queue's order of collection stays the launch order.
+cg_status collect(cg_shape_mesh* sm, Run& run, uint32_t* collected) {
+    CG_CUDA(cudaEventSynchronize(run.done));
+    const uint64_t nv = run.h_totals[0], ni = 6ull * run.h_totals[1];
+    if (nv > run.vcap || ni > run.icap) {
+        Generation& g = sm->gens[run.gen];
         CG_CUDA(cudaFreeAsync(g.verts, sm->stream));
         CG_CUDA(cudaFreeAsync(g.idx, sm->stream));
-        sm->run_vcap = nv;
-        sm->run_icap = ni;
-        CG_TRY(alloc_gen_buffers(sm, g));
-        CG_TRY(launch_run(sm));
-        CG_CUDA(cudaEventSynchronize(sm->done));
+        run.vcap = nv;
+        run.icap = ni;
+        CG_TRY(alloc_gen_buffers(sm, run, g));
+        CG_TRY(launch_run(sm, run));
+        CG_CUDA(cudaEventSynchronize(run.done));
     }
-    Generation& g = sm->gens[sm->run_gen];
-    for (size_t j = 0; j < sm->run_jobs.size(); ++j) {
-        const cg_span& sp = sm->run_jobs[j].span;
+    Generation& g = sm->gens[run.gen];
+    for (size_t j = 0; j < run.jobs.size(); ++j) {
+        const cg_span& sp = run.jobs[j].span;
         // SpanExt::center: start + (end - start) / 2 (src/octree/mod.rs:20-22)
         const V3 c = {sp.start[0] + (sp.end[0] - sp.start[0]) / 2.0f,
                       sp.start[1] + (sp.end[1] - sp.start[1]) / 2.0f,
@@ -311,9 +339,9 @@ cg_status collect(cg_shape_mesh* sm, uint32_t* collected) {
         if (i < 0) continue;
         Node& n = sm->nodes[i];
         release(sm, n);
-        const cg_job_mesh& r = sm->h_results[j];
+        const cg_job_mesh& r = run.h_results[j];
         n.status = 2;
-        n.gen = sm->run_gen;
+        n.gen = run.gen;
         n.voff = r.vertex_offset;
         n.ioff = r.index_offset;
         n.nv = r.vertices;
@@ -327,10 +355,16 @@ cg_status collect(cg_shape_mesh* sm, uint32_t* collected) {
         g.verts = nullptr;
         g.idx = nullptr;
     }
-    sm->inflight = false;
-    sm->run_jobs.clear();
-    sm->run_gen = -1;
+    run.inflight = false;
+    run.jobs.clear();
+    run.gen = -1;
     return CG_OK;
+}
+
+uint32_t jobs_in_flight(const cg_shape_mesh* sm) {
+    uint32_t n = 0;
+    for (uint32_t k : sm->queue) n += (uint32_t)sm->runs[k].jobs.size();
+    return n;
 }
 
 }  // namespace
@@ -389,9 +423,6 @@ cg_status cg_shape_mesh_create(int device, const cg_shape* shape, const cg_span*
     };
     ok(cudaStreamCreateWithFlags(&sm->stream, cudaStreamNonBlocking), "cudaStreamCreate");
     ok(cudaStreamCreateWithFlags(&sm->fstream, cudaStreamNonBlocking), "cudaStreamCreate");
-    ok(cudaEventCreateWithFlags(&sm->done, cudaEventDisableTiming), "cudaEventCreate");
-    ok(cudaMalloc(&sm->d_totals, 4 * sizeof(uint32_t)), "cudaMalloc");
-    ok(cudaMallocHost(&sm->h_totals, 4 * sizeof(uint32_t)), "cudaMallocHost");
     ok(cudaMalloc(&sm->d_rays, 9 * F2 * sizeof(float)), "cudaMalloc");
     ok(cudaMalloc(&sm->d_hit, F2), "cudaMalloc");
     ok(cudaMallocHost(&sm->h_rays, 9 * F2 * sizeof(float)), "cudaMallocHost");
@@ -414,16 +445,11 @@ void cg_shape_mesh_destroy(cg_shape_mesh* sm) {
         }
         cudaStreamSynchronize(sm->stream);
     }
-    if (sm->batch) cg_batch_destroy(sm->batch);
-    if (sm->d_results) cudaFree(sm->d_results);
-    if (sm->h_results) cudaFreeHost(sm->h_results);
-    if (sm->d_totals) cudaFree(sm->d_totals);
-    if (sm->h_totals) cudaFreeHost(sm->h_totals);
+    for (Run& run : sm->runs) free_run(run);
     if (sm->d_rays) cudaFree(sm->d_rays);
     if (sm->d_hit) cudaFree(sm->d_hit);
     if (sm->h_rays) cudaFreeHost(sm->h_rays);
     if (sm->h_hit) cudaFreeHost(sm->h_hit);
-    if (sm->done) cudaEventDestroy(sm->done);
     if (sm->fstream) cudaStreamDestroy(sm->fstream);
     if (sm->stream) cudaStreamDestroy(sm->stream);
     delete sm;
@@ -470,45 +496,48 @@ cg_status cg_shape_mesh_update(cg_shape_mesh* sm, const cg_view* view, uint32_t 
             ++s.splits;
         }
     }
-    // (2) meshes of the last run.
-    if (sm->inflight) {
-        const cudaError_t q = wait ? cudaSuccess : cudaEventQuery(sm->done);
-        if (q == cudaSuccess) {
-            CG_TRY(collect(sm, &s.collected));
-        } else if (q != cudaErrorNotReady) {
-            return cuda_status(q, "cudaEventQuery", __FILE__, __LINE__);
-        }
+    // (2) meshes of the finished runs, oldest first (with wait: all of them).
+    while (!sm->queue.empty()) {
+        Run& run = sm->runs[sm->queue.front()];
+        const cudaError_t q = wait ? cudaSuccess : cudaEventQuery(run.done);
+        if (q == cudaErrorNotReady) break;  // the later runs are behind it
+        if (q != cudaSuccess) return cuda_status(q, "cudaEventQuery", __FILE__, __LINE__);
+        CG_TRY(collect(sm, run, &s.collected));
+        sm->queue.erase(sm->queue.begin());
     }
-    // (3) a job for every empty leaf, unless a run is still in flight (its
-    // leaves are "requested"; empty leaves wait for the next update).
-    if (!sm->inflight) {
-        std::vector<int32_t> empty;
-        for (int32_t i : leaves_in_order(sm))
-            if (sm->nodes[i].status == 0) empty.push_back(i);
-        if (!empty.empty()) {
-            sm->run_jobs.clear();
-            for (int32_t i : empty) {
-                cg_span_job j{};
-                j.span = sm->nodes[i].span;
-                j.resolution = sm->res;
-                sm->run_jobs.push_back(j);
-            }
-            CG_TRY(fit_batch(sm, sm->run_jobs));
-            // A res-64 leaf of the Mandelbulb has ~1/16 of its cells on the
-            // surface at most; the run grows and repeats once if not.
-            const uint64_t r3 = (uint64_t)sm->res * sm->res * sm->res;
-            sm->run_vcap = std::max<uint64_t>(4096, empty.size() * (r3 / 16));
-            sm->run_icap = 8 * sm->run_vcap;
-            sm->gens.push_back(Generation{});
-            sm->run_gen = (int32_t)sm->gens.size() - 1;
-            CG_TRY(alloc_gen_buffers(sm, sm->gens.back()));
-            CG_TRY(launch_run(sm));
-            sm->inflight = true;
-            for (int32_t i : empty) sm->nodes[i].status = 1;
-            s.started = (uint32_t)empty.size();
+    // (3) a job for every empty leaf, in a new run queued behind the ones in
+    // flight (its leaves are "requested"); with all kMaxRuns slots in flight
+    // the empty leaves wait for a later update.
+    std::vector<int32_t> empty;
+    for (int32_t i : leaves_in_order(sm))
+        if (sm->nodes[i].status == 0) empty.push_back(i);
+    if (!empty.empty() && sm->queue.size() < kMaxRuns) {
+        uint32_t slot = 0;
+        while (sm->runs[slot].inflight) ++slot;
+        Run& run = sm->runs[slot];
+        run.jobs.clear();
+        for (int32_t i : empty) {
+            cg_span_job j{};
+            j.span = sm->nodes[i].span;
+            j.resolution = sm->res;
+            run.jobs.push_back(j);
         }
+        CG_TRY(fit_batch(sm, run, run.jobs));
+        // A res-64 leaf of the Mandelbulb has ~1/16 of its cells on the
+        // surface at most; the run grows and repeats once if not.
+        const uint64_t r3 = (uint64_t)sm->res * sm->res * sm->res;
+        run.vcap = std::max<uint64_t>(4096, empty.size() * (r3 / 16));
+        run.icap = 8 * run.vcap;
+        sm->gens.push_back(Generation{});
+        run.gen = (int32_t)sm->gens.size() - 1;
+        CG_TRY(alloc_gen_buffers(sm, run, sm->gens.back()));
+        CG_TRY(launch_run(sm, run));
+        run.inflight = true;
+        sm->queue.push_back(slot);
+        for (int32_t i : empty) sm->nodes[i].status = 1;
+        s.started = (uint32_t)empty.size();
     }
-    s.active = sm->inflight ? (uint32_t)sm->run_jobs.size() : 0;
+    s.active = jobs_in_flight(sm);
     s.leaves = (uint32_t)leaves_in_order(sm).size();
     if (stats) *stats = s;
     return CG_OK;

@@ -392,13 +392,15 @@ typedef struct cg_lod_stats {
  * (1) the 5 x 5 focus rays are marched on the GPU (100 steps, hit when
  *     DE < 1e-6) and every READY leaf around a hit closer to the camera than
  *     twice the leaf's width is split into eight empty leaves;
- * (2) if the previous update's jobs have finished (or, with wait != 0,
- *     after waiting for them) their meshes become ready, each in the leaf
- *     around its span's centre;
+ * (2) the meshes of the runs that have finished (with wait != 0, of all
+ *     runs, after waiting for them) become ready, each in the leaf around
+ *     its span's centre; runs are collected in the order they started;
  * (3) every empty leaf becomes a job: all of them are meshed by one batched
  *     persistent launch chain (the thread pool's generate_for_box jobs),
- *     asynchronously; those leaves are "requested" until a later update
- *     collects them.
+ *     asynchronously, queued behind the runs still in flight (at most four
+ *     runs at a time; beyond that the empty leaves wait for a later
+ *     update); those leaves are "requested" until a later update collects
+ *     them.
  * stats may be NULL. */
 cg_status cg_shape_mesh_update(cg_shape_mesh* sm, const cg_view* view, uint32_t wait,
                                cg_lod_stats* stats);

@@ -132,6 +132,37 @@ def test_update_without_wait_collects_later(cg):
     sm.close()
 
 
+def test_update_takes_jobs_while_runs_are_in_flight(cg):
+    """Like the reference's thread pool, which accepts jobs while older ones
+    run: an update starts a run for newly empty leaves although an earlier
+    run is still in flight (res-256 leaves, so the first run takes tens of
+    milliseconds); later updates collect the runs in launch order, and every
+    ready leaf ends with the mesh of its own span."""
+    from cantucci_gb300.lod import Camera, EMPTY, REQUESTED
+    sm = make(cg, cg.Mandelbulb(8, 15, 2.5), res=256)
+    far = Camera(position=(0, -30, 0), direction=(0, 1, 0))
+    sm.update(far, wait=True)
+    sm.update(far, wait=True)
+    near = [Camera(position=(0.05, -1.45, 0.1), direction=(0, 1, 0.05)),
+            Camera(position=(-0.3, -1.25, 0.2), direction=(0.2, 1, -0.1)),
+            Camera(position=(0.4, -1.3, -0.2), direction=(-0.2, 1, 0.1))]
+    stats = [sm.update(cam, wait=False) for cam in near]
+    started = [st["started"] for st in stats]
+    assert started[0] > 0 and sum(started[1:]) > 0, started
+    # a run started while the first one was still queued or running
+    overlapped = [k for k in (1, 2) if started[k] > 0 and stats[k]["collected"] == 0
+                  and stats[k]["active"] > started[k]]
+    assert overlapped, stats
+    assert all(l.status in (EMPTY, REQUESTED) or l.ready for l in sm.leaves())
+    for _ in range(4):  # from far away nothing splits: collect, mesh the rest, collect
+        st = sm.update(far, wait=True)
+        if st["started"] == 0 and st["active"] == 0:
+            break
+    assert all(l.ready for l in sm.leaves())
+    assert check_meshes(cg, sm, 256, limit=6) == 6
+    sm.close()
+
+
 def test_polar_shape_and_bad_arguments(cg):
     from cantucci_gb300 import CantucciError
     from cantucci_gb300.lod import Camera, ShapeMesh
