@@ -408,11 +408,12 @@ def test_root_crossings(cg, shape_kind):
 
 
 @pytest.mark.slow
-def test_max_resolution_span(cg):
+def test_max_resolution_span(cg, orc):
     """Resolution 1024 (the largest the ABI takes: 1025^3 corners, a 4.3 GB
-    distance grid): the mesh completes, every index refers to a vertex, and
+    distance grid): the mesh completes, every index refers to a vertex,
     sampled corners of the grid equal the point estimator at the same
-    coordinates bit for bit."""
+    coordinates bit for bit, and the oracle's steps 2-3 on the GPU's own
+    distances give the same index list and vertex positions bit for bit."""
     import torch
     s = cg.Mandelbulb(8, 15, 2.5)
     span = cg.Span([-1.2] * 3, [1.2] * 3)
@@ -438,6 +439,10 @@ def test_max_resolution_span(cg):
         want = s.batch_min_distance_from(pts)
         got = d[cells[:, 0], cells[:, 1], cells[:, 2]].cpu().numpy()
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+        del d
+        a = v[:nv].cpu().numpy()
+        ih = i[:ni].cpu().numpy().view(np.uint32)
+        placement_vs_oracle(orc, m, a, ih, res, m.last_status)
     finally:
         m.close()
 
