@@ -198,6 +198,87 @@ __global__ void __launch_bounds__(128) k_place(ShapeDev s, PlaceParams pp, MeshD
     if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
 }
 
+// Small spans: the seven samples of a vertex on seven lanes of a group of
+// eight (four vertices per warp), so a vertex waits for one estimator call
+// instead of seven in a row; lane 0 of the group forms the record.  The
+// same operations as k_place<M, false, false, false>, so the same bits.
+// The loop bound is warp-uniform, so every lane reaches the shuffles.
+template <int M>
+__global__ void __launch_bounds__(128) k_place_spread(ShapeDev s, PlaceParams pp, MeshDims d,
+                                                      const float* __restrict__ dists,
+                                                      const uint32_t* __restrict__ cellidx,
+                                                      MeshCounters* __restrict__ cnt,
+                                                      cg_vertex* __restrict__ verts,
+                                                      uint64_t vcap,
+                                                      const PlaceParams* __restrict__ ppp) {
+    if (ppp) pp = *ppp;
+    const uint32_t V = cnt->vertices;
+    const uint32_t lane = threadIdx.x & 31, k = lane & 7, g0 = lane & ~7u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    float* vf = reinterpret_cast<float*>(verts);
+    bool bad = false;
+    for (uint32_t base = warp * 4; base < V; base += nwarps * 4) {
+        const uint32_t v = base + (lane >> 3);
+        const bool live = v < V;
+        float vx = 0.0f, vy = 0.0f, vz = 0.0f, val = 0.0f;
+        if (live) {
+            CellCrossings cc;
+            cell_crossings(pp, d, dists, CG_AT(cellidx, v, (uint64_t)d.res * d.res * d.res), cc);
+            const float cf = (float)cc.count;
+            vx = __fadd_rn(0.0f, __fdiv_rn(cc.sx, cf));
+            vy = __fadd_rn(0.0f, __fdiv_rn(cc.sy, cf));
+            vz = __fadd_rn(0.0f, __fdiv_rn(cc.sz, cf));
+            if (k == 0) bad |= cc.bad;
+            if (k < 7) {
+                float qx, qy, qz;
+                sample_point(pp, (int)k, vx, vy, vz, qx, qy, qz);
+                val = eval<M>(s, qx, qy, qz);
+            }
+        }
+        float de[7];
+#pragma unroll
+        for (int j = 0; j < 7; ++j) de[j] = __shfl_sync(0xFFFFFFFFu, val, g0 + j);
+        if (live && k == 0 && v < vcap) {
+            float o[7];
+            vertex_record(de, vx, vy, vz, o);
+#pragma unroll
+            for (int j = 0; j < 7; ++j) CG_AT(vf, (uint64_t)v * 7 + j, vcap * 7) = o[j];
+        }
+    }
+    if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
+}
+
+// Spans up to this resolution place with k_place_spread: their few
+// thousand vertices leave most of the GPU idle, so the seven estimator
+// calls in a row are the placement's time.
+constexpr uint32_t kSpreadMaxRes = 64;
+
+// One resident wave of k_place_spread blocks, and no more than the span's
+// cells can fill (four vertices per warp).
+template <int M>
+static unsigned spread_grid(const MeshDims& d) {
+    static int per_sm = 0;
+    if (!per_sm) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_place_spread<M>, 128, 0) !=
+                cudaSuccess || b < 1)
+            b = 1;
+        per_sm = b;
+    }
+    const uint64_t cap = (uint64_t)sm_count() * per_sm;
+    const uint64_t need = ((uint64_t)d.res * d.res * d.res + 15) / 16;  // 16 vertices a block
+    return (unsigned)(need < cap ? need : cap);
+}
+
+template <int M>
+static void launch_place_spread(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
+                                const MeshWork& w, cg_vertex* verts, uint64_t vcap,
+                                cudaStream_t st, const PlaceParams* pp_dev) {
+    k_place_spread<M><<<spread_grid<M>(d), 128, 0, st>>>(s, pp, d, w.dists, w.cellidx,
+                                                         w.counters, verts, vcap, pp_dev);
+}
+
 // Edge table, pass 1: per row r = a n^2 + x n + y (axis a, corner row
 // (x, y)), the sign-changing edges before each word and in the row.
 __global__ void __launch_bounds__(256) k_edge_rows(const uint32_t* __restrict__ sgn, MeshDims d,
@@ -388,6 +469,8 @@ static void launch_place_mode(const ShapeDev& s, const PlaceParams& pp, const Me
     else if (opt.root_iters)
         k_place<M, AN, true, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                      verts, vcap, opt.root_iters, et, opt.pp_dev);
+    else if (!AN && d.res <= kSpreadMaxRes)
+        launch_place_spread<M>(s, pp, d, w, verts, vcap, st, opt.pp_dev);
     else
         k_place<M, AN, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,
                                                       verts, vcap, 0, et, opt.pp_dev);
@@ -488,6 +571,10 @@ template <int M>
 static void launch_place_plain(const ShapeDev& s, const PlaceParams& pp, const MeshDims& d,
                                const MeshWork& w, cg_vertex* verts, uint64_t vcap,
                                cudaStream_t st, const PlaceParams* pp_dev) {
+    if (d.res <= kSpreadMaxRes) {
+        launch_place_spread<M>(s, pp, d, w, verts, vcap, st, pp_dev);
+        return;
+    }
     const unsigned B = 128;
     const unsigned G = place_grid(d, B);
     k_place<M, false, false, false><<<G, B, 0, st>>>(s, pp, d, w.dists, w.cellidx, w.counters,

@@ -239,41 +239,106 @@ __device__ __forceinline__ float linear_root(float f0, float f1) {
 // edge midpoint); ROOT is then unused.
 // Neither changes the cell table or the index list.
 // Returns false if a lerp factor left [0, 1] (src/math.rs:19 panics there).
+// Cell c's corner distances, its corner p0, and its sign-changing edges'
+// lerp crossings summed in EDGES order (buffer.rs:187-250); `bad` when a
+// lerp factor left [0, 1].
+struct CellCrossings {
+    uint32_t x, y, z;
+    float dd[8];
+    float p0x, p0y, p0z;
+    float sx, sy, sz;
+    uint32_t count, xmask;
+    bool bad;
+};
+
+__device__ __forceinline__ void cell_crossings(const PlaceParams& pp, const MeshDims& d,
+                                               const float* __restrict__ dists, uint32_t c,
+                                               CellCrossings& q) {
+    q.z = c % d.res;
+    const uint32_t xy = c / d.res;
+    q.y = xy % d.res;
+    q.x = xy / d.res;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t cx = q.x + ((k >> 2) & 1), cy = q.y + ((k >> 1) & 1), cz = q.z + (k & 1);
+        q.dd[k] = CG_AT(dists, ((size_t)cx * d.n + cy) * d.n + cz, (uint64_t)d.n * d.n * d.n);
+    }
+    q.p0x = __fadd_rn(pp.start[0], __fmul_rn((float)q.x, pp.step[0]));
+    q.p0y = __fadd_rn(pp.start[1], __fmul_rn((float)q.y, pp.step[1]));
+    q.p0z = __fadd_rn(pp.start[2], __fmul_rn((float)q.z, pp.step[2]));
+    // EDGES (buffer.rs:155-176): x edges, y edges, z edges.
+    const uint8_t EF[12] = {0, 1, 2, 3, 0, 1, 4, 5, 0, 2, 4, 6};
+    const uint8_t ET[12] = {4, 5, 6, 7, 2, 3, 6, 7, 1, 3, 5, 7};
+    q.sx = q.sy = q.sz = 0.0f;
+    q.count = q.xmask = 0;
+    q.bad = false;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+        const int from = EF[k], to = ET[k];
+        const float df0 = q.dd[from], dt0 = q.dd[to];
+        if ((__float_as_uint(df0) >> 31) == (__float_as_uint(dt0) >> 31)) continue;
+        q.xmask |= 1u << k;
+        float cx, cy, cz;
+        lerp_crossing(pp, q.p0x, q.p0y, q.p0z, from, to, df0, dt0, q.bad, cx, cy, cz);
+        q.sx = __fadd_rn(q.sx, cx);
+        q.sy = __fadd_rn(q.sy, cy);
+        q.sz = __fadd_rn(q.sz, cz);
+        ++q.count;
+    }
+}
+
+// Sample k of a vertex (buffer.rs:254-266): 0 is the vertex itself; 1..6
+// are p + unit * (+-delta) along x, y, z, i.e. p + (delta, +0, +0) and
+// p + (-delta, -0, -0) etc.
+__device__ __forceinline__ void sample_point(const PlaceParams& pp, int k, float vx, float vy,
+                                             float vz, float& qx, float& qy, float& qz) {
+    qx = vx;
+    qy = vy;
+    qz = vz;
+    if (k > 0) {
+        const int axis = (k - 1) >> 1;
+        const bool neg = ((k - 1) & 1) != 0;
+        const float zero = neg ? -0.0f : 0.0f;
+        const float dd0 = axis == 0 ? pp.delta[0] : (axis == 1 ? pp.delta[1] : pp.delta[2]);
+        const float off = neg ? -dd0 : dd0;
+        qx = __fadd_rn(vx, axis == 0 ? off : zero);
+        qy = __fadd_rn(vy, axis == 1 ? off : zero);
+        qz = __fadd_rn(vz, axis == 2 ? off : zero);
+    }
+}
+
+// The vertex record from its position and its seven samples' distances:
+// the normal is cgmath's normalize of the central differences,
+// v * (1 / |v|) with |v| = sqrt((x*x + y*y) + z*z).
+__device__ __forceinline__ void vertex_record(const float (&de)[7], float vx, float vy, float vz,
+                                              float* __restrict__ o) {
+    const float nx = __fsub_rn(de[1], de[2]);
+    const float ny = __fsub_rn(de[3], de[4]);
+    const float nz = __fsub_rn(de[5], de[6]);
+    const float inv = __fdiv_rn(1.0f, magnitude<Exact>(nx, ny, nz));
+    o[0] = vx;
+    o[1] = vy;
+    o[2] = vz;
+    o[3] = __fmul_rn(nx, inv);
+    o[4] = __fmul_rn(ny, inv);
+    o[5] = __fmul_rn(nz, inv);
+    o[6] = de[0];
+}
+
 template <int M, bool AN = false, bool ROOT = false, bool QEF = false>
 __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParams& pp,
                                              const MeshDims& d, const float* __restrict__ dists,
                                              uint32_t c, float* __restrict__ o,
                                              uint32_t root_iters = 0,
                                              const EdgeTable* et = nullptr) {
-    const uint32_t z = c % d.res, xy = c / d.res, y = xy % d.res, x = xy / d.res;
-    float dd[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const uint32_t cx = x + ((k >> 2) & 1), cy = y + ((k >> 1) & 1), cz = z + (k & 1);
-        dd[k] = CG_AT(dists, ((size_t)cx * d.n + cy) * d.n + cz, (uint64_t)d.n * d.n * d.n);
-    }
-    const float p0x = __fadd_rn(pp.start[0], __fmul_rn((float)x, pp.step[0]));
-    const float p0y = __fadd_rn(pp.start[1], __fmul_rn((float)y, pp.step[1]));
-    const float p0z = __fadd_rn(pp.start[2], __fmul_rn((float)z, pp.step[2]));
-    // EDGES (buffer.rs:155-176): x edges, y edges, z edges.
-    const uint8_t EF[12] = {0, 1, 2, 3, 0, 1, 4, 5, 0, 2, 4, 6};
-    const uint8_t ET[12] = {4, 5, 6, 7, 2, 3, 6, 7, 1, 3, 5, 7};
-    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
-    uint32_t count = 0, xmask = 0;
-    bool bad = false;
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-        const int from = EF[k], to = ET[k];
-        const float df0 = dd[from], dt0 = dd[to];
-        if ((__float_as_uint(df0) >> 31) == (__float_as_uint(dt0) >> 31)) continue;
-        xmask |= 1u << k;
-        float cx, cy, cz;
-        lerp_crossing(pp, p0x, p0y, p0z, from, to, df0, dt0, bad, cx, cy, cz);
-        sx = __fadd_rn(sx, cx);
-        sy = __fadd_rn(sy, cy);
-        sz = __fadd_rn(sz, cz);
-        ++count;
-    }
+    CellCrossings cc;
+    cell_crossings(pp, d, dists, c, cc);
+    const uint32_t x = cc.x, y = cc.y, z = cc.z;
+    const float(&dd)[8] = cc.dd;
+    const float p0x = cc.p0x, p0y = cc.p0y, p0z = cc.p0z;
+    float sx = cc.sx, sy = cc.sy, sz = cc.sz;
+    const uint32_t count = cc.count, xmask = cc.xmask;
+    const bool bad = cc.bad;
     if constexpr (ROOT && !QEF) {
         sx = sy = sz = 0.0f;
 #pragma unroll 1
@@ -333,9 +398,8 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
         vy = p0y + ry;
         vz = p0z + rz;
     }
-    // Sample 0 is the vertex; samples 1..6 are p + unit * (+-delta) along
-    // x, y, z, i.e. p + (delta, +0, +0) and p + (-delta, -0, -0) etc.  The
-    // loop is kept rolled so that one copy of the estimator is in the code.
+    // The seven samples (sample_point) one after another; the loop is kept
+    // rolled so that one copy of the estimator is in the code.
     if constexpr (AN) {
         float g[4];
         shape_gradient<M>(s, vx, vy, vz, g);
@@ -355,35 +419,13 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
         float de[7];
 #pragma unroll 1
         for (int k = 0; k < 7; ++k) {
-            float qx = vx, qy = vy, qz = vz;
-            if (k > 0) {
-                const int axis = (k - 1) >> 1;
-                const bool neg = ((k - 1) & 1) != 0;
-                const float zero = neg ? -0.0f : 0.0f;
-                const float dd0 = axis == 0 ? pp.delta[0] : (axis == 1 ? pp.delta[1] : pp.delta[2]);
-                const float off = neg ? -dd0 : dd0;
-                qx = __fadd_rn(vx, axis == 0 ? off : zero);
-                qy = __fadd_rn(vy, axis == 1 ? off : zero);
-                qz = __fadd_rn(vz, axis == 2 ? off : zero);
-            }
+            float qx, qy, qz;
+            sample_point(pp, k, vx, vy, vz, qx, qy, qz);
             const float val = eval<M>(s, qx, qy, qz);
 #pragma unroll
             for (int j = 0; j < 7; ++j) de[j] = (j == k) ? val : de[j];
         }
-        const float nx = __fsub_rn(de[1], de[2]);
-        const float ny = __fsub_rn(de[3], de[4]);
-        const float nz = __fsub_rn(de[5], de[6]);
-        // cgmath normalize: v * (1 / |v|), |v| = sqrt((x*x + y*y) + z*z).
-        const float inv = __fdiv_rn(1.0f, magnitude<Exact>(nx, ny, nz));
-        if (o) {
-            o[0] = vx;
-            o[1] = vy;
-            o[2] = vz;
-            o[3] = __fmul_rn(nx, inv);
-            o[4] = __fmul_rn(ny, inv);
-            o[5] = __fmul_rn(nz, inv);
-            o[6] = de[0];
-        }
+        if (o) vertex_record(de, vx, vy, vz, o);
         return !bad;
     }
 }
