@@ -378,6 +378,36 @@ __global__ void __launch_bounds__(256) k_quad_emit(const uint32_t* __restrict__ 
                       icap, r);
 }
 
+// Small spans: one warp per (corner row, sign word), one lane per corner.
+// A lane's first quad is the row's offset, plus the quads of the row's
+// earlier words, plus those of the word's corners below it; the lane then
+// emits its corner's (at most three) quads.  The same list as k_quad_emit
+// with a corner's quads, not a row's, in a row.
+__global__ void __launch_bounds__(256) k_quad_emit_fine(const uint32_t* __restrict__ sgn,
+                                                        MeshDims d, const float* __restrict__ dists,
+                                                        const uint32_t* __restrict__ cellbits,
+                                                        const uint32_t* __restrict__ wordoff,
+                                                        const uint32_t* __restrict__ rowoff,
+                                                        const uint32_t* __restrict__ quadoff,
+                                                        uint32_t* __restrict__ idx, uint64_t icap) {
+    const uint32_t rows = d.res * d.res, units = rows * d.Wc;
+    const uint32_t lane = threadIdx.x & 31, bit = 1u << lane;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units; u += nwarps) {
+        const uint32_t r = u / d.Wc, w = u % d.Wc, x = r / d.res, y = r % d.res;
+        uint64_t q = CG_AT(quadoff, r, rows);
+        for (uint32_t w2 = 0; w2 < w; ++w2) {
+            const EdgeWords e2 = edge_words(sgn, d, x, y, w2);
+            q += __popc(e2.ex) + __popc(e2.ey) + __popc(e2.ez);
+        }
+        const EdgeWords e = edge_words(sgn, d, x, y, w);
+        const uint32_t below = bit - 1u;
+        q += __popc(e.ex & below) + __popc(e.ey & below) + __popc(e.ez & below);
+        const EdgeWords mine = {e.ex & bit, e.ey & bit, e.ez & bit};
+        quad_emit_word(mine, d, dists, cellbits, wordoff, rowoff, 0u, q, idx, icap, x, y, w);
+    }
+}
+
 // Copy of the first n words of src (n <= src_cap) to dst (n <= dst_cap),
 // both 16-byte aligned, as 16-byte units: the quad indices into mapped host
 // memory.  A few blocks keep the link busy; beside the placement they cost
@@ -647,6 +677,14 @@ static cg_status launch_quad_count(const MeshDims& d, const MeshWork& w, cudaStr
 
 static cg_status launch_quad_emit(const MeshDims& d, const MeshWork& w, uint32_t* idx,
                                   uint64_t icap, cudaStream_t st) {
+    if (d.res <= kSpreadMaxRes) {
+        const uint64_t lanes = (uint64_t)d.res * d.res * d.Wc * 32;
+        const unsigned B = 256, G = grid_for(lanes, B, 8);
+        k_quad_emit_fine<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff,
+                                          w.quadoff, idx, icap);
+        CG_CHECK_LAUNCH("k_quad_emit_fine");
+        return CG_OK;
+    }
     const uint32_t rows = d.res * d.res;
     const unsigned B = 256, G = grid_for(rows, B, 8);
     k_quad_emit<<<G, B, 0, st>>>(w.sgn, d, w.dists, w.cellbits, w.wordoff, w.rowoff, w.quadoff,
