@@ -249,9 +249,11 @@ __global__ void __launch_bounds__(128) k_place_spread(ShapeDev s, PlaceParams pp
     if (bad) atomicOr(&cnt->status, MESH_LERP_FAIL);
 }
 
-// Spans up to this resolution place with k_place_spread: their few
-// thousand vertices leave most of the GPU idle, so the seven estimator
-// calls in a row are the placement's time.
+// Spans up to this resolution place with k_place_spread and emit quads with
+// k_quad_emit_fine: their few thousand vertices leave most of the GPU
+// idle, so the seven estimator calls in a row and a row's quads in a row
+// are the time.  (At res 128 the pair measured slower: 0.180 against
+// 0.169 ms per mesh.)
 constexpr uint32_t kSpreadMaxRes = 64;
 
 // One resident wave of k_place_spread blocks, and no more than the span's
