@@ -107,11 +107,11 @@ __global__ void __launch_bounds__(256) k_cells(const uint32_t* __restrict__ sgn,
         const uint32_t r = r0 + g.lane_row;
         const bool ok = r < rows;
         const uint32_t surf = ok ? cells_word(sgn, d, r, g.sub) : 0u;
-        const uint32_t cnt = __popc(surf);
-        const uint32_t inc = group_inclusive_scan(cnt, g.sub, g.L);
+        const uint32_t here = __popc(surf);
+        const uint32_t inc = group_inclusive_scan(here, g.sub, g.L);
         if (ok) {
             CG_AT(cellbits, r * d.Wc + g.sub, nc) = surf;
-            CG_AT(wordoff, r * d.Wc + g.sub, nc) = inc - cnt;
+            CG_AT(wordoff, r * d.Wc + g.sub, nc) = inc - here;
             if (g.sub == g.L - 1) CG_AT(rowcnt, r, rows) = inc;
         }
     }
