@@ -323,7 +323,12 @@ static void launch_grid_mode(const ShapeDev& s, const GridDev& g, float* out, ui
                              uint32_t W, cudaStream_t st, const GridDev* gp) {
     const unsigned B = 256;
     int k = g_de_grid_kernel;
-    if (k == DE_GRID_AUTO) k = g.n >= 33 ? DE_GRID_BRICK : DE_GRID_LINEAR;
+    // Up to 65^3 corners (res 64, cantucci's leaves) one corner per thread:
+    // a warp's DE chain is then the whole time (about 12 us for one
+    // 15-iteration evaluation at low occupancy), and the linear kernel's 45
+    // registers (5 resident blocks per SM) fit the grid in fewer waves than
+    // the bricks' 72 (3 blocks): 19.6 against 23.5 us for the res-64 grid.
+    if (k == DE_GRID_AUTO) k = g.n > 65 ? DE_GRID_BRICK : DE_GRID_LINEAR;
     if (k == DE_GRID_PACKED && (M == MODE_P8 || M == MODE_P8_IT15)) {
         const uint64_t b4 = (g.n + 3) >> 2;
         k_de_grid_p8x2<<<grid_for(b4 * b4 * b4 * 32, B, 8), B, 0, st>>>(s, g, out, sgn, W, gp);
