@@ -70,11 +70,12 @@ def placement_vs_oracle(orc, mesher, a, indices, res, status):
     and their centroid, buffer.rs:187-250) and the quads follow from the
     distances alone, so they must match bit for bit.  Only the estimator
     calls at the vertex differ, through CUDA's logf against glibc's: the two
-    ln r are within 1.5 ulp (CUDA's logf is within 1 ulp, glibc's within
-    half an ulp), and the product by r and the quotient by dr round once
-    more on each side, so the distances at the vertex are within
-    (1.5 + 1 + 1) 2^-23 relative, 7 ulp; 99% must be within 2 ulp.  The
-    six-sample normal within 0.1 degree for 99.9%."""
+    ln r are within 1.82 ulp (CUDA's logf is within 1 ulp, glibc's within
+    0.82), and the product by r and the quotient by dr round once more on
+    each side (half an ulp each), so the distances at the vertex differ by
+    less than (1.82 + 1 + 1) 2^-23 relative, which is under 8 ulp: at most
+    7; 99% must be within 2 ulp.  The six-sample normal within 0.1 degree
+    for 99.9%."""
     d = mesher.last_dists().cpu().numpy()
     ref = orc.mesh_from_dists(orc.mandelbulb(8, 15, 2.5), np.array(W.SPAN_C1).ravel(), res, d,
                               vcap=len(a) + 1, icap=len(indices) + 1)

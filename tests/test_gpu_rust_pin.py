@@ -7,9 +7,10 @@ Bar:
     makes carry x86's 0xFFC00000), values within 7 ulp and 99% within 2;
     the loop state is bit-identical, and the final 0.5 (ln r) r / dr
     differs only through ln r: CUDA's logf is within 1 ulp and glibc's
-    within half an ulp, so the two ln r are within 1.5 ulp, and the product
-    and the quotient that follow round once more on each side, which bounds
-    the difference by (1.5 + 1 + 1) 2^-23 relative, 7 ulp; the cell table
+    within 0.82, so the two ln r are within 1.82 ulp, and the product and
+    the quotient that follow round once more on each side (half an ulp
+    each), which keeps the difference below (1.82 + 1 + 1) 2^-23 relative,
+    under 8 ulp: at most 7; the cell table
     and index list of every mesh bit for bit, and the sign of every corner
     distance;
   - Sphere (no libm): distances and whole meshes, vertices included, bit for
