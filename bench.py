@@ -56,19 +56,22 @@ def fp32_peak(packed: bool = False) -> float:
     return out.value
 
 
-def ncu_record(kernel: str, res: int):
+def ncu_record(kernel: str, res: int, pdir: str = None, digest: str = None):
     """The ncu figures of `kernel` at `res` recorded for THIS build, or None.
     A profile summary under profiles/ carries a line
         bench-record: digest=<16 hex> kernel=<name> res=<n> dram_bytes=<b> ...
     whose digest is the library build digest the capture ran on; a record of
-    another build (any changed source) is ignored."""
-    from cantucci_gb300 import build
-    stamp = os.path.join(build.LIB_DIR, ".digest")
-    try:
-        digest = open(stamp).read().strip()[:16]
-    except OSError:
-        return None
-    pdir = os.path.join(ROOT, "profiles")
+    another build (any changed source) is ignored.  `pdir` and `digest`
+    default to profiles/ and the built library's digest."""
+    if digest is None:
+        from cantucci_gb300 import build
+        stamp = os.path.join(build.LIB_DIR, ".digest")
+        try:
+            digest = open(stamp).read().strip()
+        except OSError:
+            return None
+    digest = digest[:16]
+    pdir = pdir or os.path.join(ROOT, "profiles")
     for name in sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []:
         if not name.endswith(".md"):
             continue
