@@ -225,6 +225,14 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
                 break;
             }
             ++steps;
+            // Once |z| is NaN every later iterate is NaN (each component of
+            // the next z takes a NaN operand), r stays NaN, nothing escapes,
+            // and the distance is NaN whatever the remaining steps do.  The
+            // origin gets there in its second step (acos(0/0) on the z axis)
+            // and would otherwise run all its steps through the division's
+            // and square root's special-case paths; without the loop state
+            // (st), stop there.  One test in the unrolled loop.
+            if (i == 1 && !st && r != r) break;
         }
     } else {
         for (uint32_t i = 0; i < max_iters; ++i) {
