@@ -208,7 +208,7 @@ __device__ __forceinline__ bool mandelbulb_step(int32_t P, float Pf, float bailo
 // out: it is |z| at the start of the last iteration.  FIXED > 0 is a
 // compile-time max_iters: the loop is unrolled, which drops the trip-count
 // test from every iteration (same operations, same bits).
-template <class O, bool P8, int FIXED = 0>
+template <class O, bool P8, int FIXED = 0, bool NAN_EXIT = false>
 __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, float bailout,
                                                float px, float py, float pz,
                                                MbState* st = nullptr) {
@@ -225,14 +225,16 @@ __device__ __forceinline__ float mandelbulb_de(int32_t P, uint32_t max_iters, fl
                 break;
             }
             ++steps;
-            // Once |z| is NaN every later iterate is NaN (each component of
-            // the next z takes a NaN operand), r stays NaN, nothing escapes,
-            // and the distance is NaN whatever the remaining steps do.  The
-            // origin gets there in its second step (acos(0/0) on the z axis)
-            // and would otherwise run all its steps through the division's
-            // and square root's special-case paths; without the loop state
-            // (st), stop there.  One test in the unrolled loop.
-            if (i == 1 && !st && r != r) break;
+            // NAN_EXIT: once |z| is NaN every later iterate is NaN (each
+            // component of the next z takes a NaN operand), r stays NaN,
+            // nothing escapes, and the distance is NaN whatever the
+            // remaining steps do.  The origin gets there in its second step
+            // (acos(0/0) on the z axis) and would otherwise run all its steps
+            // through the division's and square root's special-case paths,
+            // which sets the time of a small grid; stop there.  Only for
+            // callers that want the distance alone (the loop state differs).
+            if constexpr (NAN_EXIT)
+                if (i == 1 && r != r) break;
         }
     } else {
         for (uint32_t i = 0; i < max_iters; ++i) {
@@ -666,10 +668,12 @@ enum Mode {
     MODE_P8_FAST_IT15 = 8  // MODE_P8_FAST likewise
 };
 
-template <int M>
+// NAN_EXIT: the unrolled P=8 loop stops at a NaN second step (same bits).
+template <int M, bool NAN_EXIT = false>
 __device__ __forceinline__ float eval(const ShapeDev& s, float x, float y, float z) {
     if (M == MODE_P8) return mandelbulb_de<Exact, true>(8, s.max_iters, s.bailout, x, y, z);
-    if (M == MODE_P8_IT15) return mandelbulb_de<Exact, true, 15>(8, 15, s.bailout, x, y, z);
+    if (M == MODE_P8_IT15)
+        return mandelbulb_de<Exact, true, 15, NAN_EXIT>(8, 15, s.bailout, x, y, z);
     if (M == MODE_INT) return mandelbulb_de<Exact, false>(s.power, s.max_iters, s.bailout, x, y, z);
     if (M == MODE_POLAR) return polar_de(s, x, y, z);
     if (M == MODE_SPHERE) return sphere_de(s, x, y, z);

@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) k_de_grid(ShapeDev s, GridDev g, float* _
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
         float x, y, z;
         grid_point(g, i, x, y, z);
-        const float d = eval<M>(s, x, y, z);
+        const float d = eval<M, true>(s, x, y, z);
         CG_AT(out, i, total) = d;
         if (sgn && !(__float_as_uint(d) >> 31)) {
             const uint32_t zi = i % g.n, row = i / g.n;
