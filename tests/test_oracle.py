@@ -152,6 +152,37 @@ def test_mesh_topology_invariants(orc):
     assert np.array_equal(pts[surf], np.arange(m["nv"], dtype=np.uint32))
 
 
+@pytest.mark.parametrize("shape,res", [("p8", 32), ("p8", 64), ("sphere", 16)])
+def test_mesh_from_dists_reproduces_the_mesher(orc, shape, res):
+    """Steps 2-3 on given corner distances (the entry the GPU parity tests
+    feed with the GPU's own grid) reproduce generate_for_box bit for bit when
+    given its own step-1 grid; a changed distance changes the mesh there."""
+    s = orc.mandelbulb(8, 15, 2.5) if shape == "p8" else orc.sphere((0.1, -0.05, 0.02), 0.9)
+    span = np.array(W.SPAN_C1, np.float32).ravel()
+    full = orc.generate_for_box(s, span, res, want_grids=True)
+    again = orc.mesh_from_dists(s, span, res, full["dists"])
+    assert again["rc"] == full["rc"] and (again["nv"], again["ni"]) == (full["nv"], full["ni"])
+    assert np.array_equal(again["indices"], full["indices"])
+    assert np.array_equal(again["points"], full["points"])
+    assert np.array_equal(again["vertices"].view(np.uint8), full["vertices"].view(np.uint8))
+    # flip the sign of one inside corner next to the surface: the cell table moves
+    d = full["dists"].copy().reshape(-1)
+    k = int(np.flatnonzero((d < 0) & (d > -0.05))[0])
+    d[k] = -d[k]
+    moved = orc.mesh_from_dists(s, span, res, d)
+    assert not np.array_equal(moved["points"], full["points"])
+
+
+def test_mesh_from_dists_rejects_a_null_grid(orc):
+    import ctypes as C
+    lib = orc.lib()
+    nv, ni = C.c_uint64(), C.c_uint64()
+    span = np.array(W.SPAN_C1, np.float32).ravel()
+    rc = lib.orc_mesh_from_dists(C.byref(orc.mandelbulb(8, 15, 2.5)), span.ctypes.data, 8, 1,
+                                 None, None, None, 0, None, 0, C.byref(nv), C.byref(ni))
+    assert rc == orc.ORC_EINVAL
+
+
 def test_sphere_vertices_near_surface(orc):
     c, r = np.array([0.1, -0.2, 0.05], np.float32), 0.9
     m = orc.generate_for_box(orc.sphere(c, r), np.array([-1, -1, -1, 1, 1, 1], np.float32), 32)
