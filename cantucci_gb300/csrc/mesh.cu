@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) k_cells(const uint32_t* __restrict__ sgn,
         cnt->edges = 0;
     }
     const uint32_t rows = d.res * d.res;
-    const uint64_t nc = (uint64_t)rows * d.Wc;
+    [[maybe_unused]] const uint64_t nc = (uint64_t)rows * d.Wc;
     const RowLanes g(d);
     for (uint32_t r0 = g.warp * g.per_warp; r0 < rows; r0 += g.nwarps * g.per_warp) {
         const uint32_t r = r0 + g.lane_row;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_vertex_list(MeshDims d, const uint32_t*
                                                      const uint32_t* __restrict__ rowoff,
                                                      uint32_t* __restrict__ cellidx) {
     const uint32_t rows = d.res * d.res;
-    const uint64_t nc = (uint64_t)rows * d.Wc;
+    [[maybe_unused]] const uint64_t nc = (uint64_t)rows * d.Wc;
 #ifdef CG_CHECKED
     const uint64_t cap = (uint64_t)rows * d.res;
 #endif
@@ -412,14 +412,22 @@ __global__ void __launch_bounds__(256) k_quad_emit_fine(const uint32_t* __restri
 
 // Copy of the first n words of src (n <= src_cap) to dst (n <= dst_cap),
 // both 16-byte aligned, as 16-byte units: the quad indices into mapped host
-// memory.  A few blocks keep the link busy; beside the placement they cost
-// less than a copy-engine transfer, whose traffic competes with the
-// placement's own stores into host memory.
+// memory.  With `cnt`, n is read on the device instead: the mesh's
+// 6 * quads, cut at dst_cap, so the copy needs no count on the host.  A few
+// blocks keep the link busy; beside the placement they cost less than a
+// copy-engine transfer, whose traffic competes with the placement's own
+// stores into host memory.
 static constexpr unsigned kCopyBlocks = 16;
 
 __global__ void __launch_bounds__(256) k_copy_words(const uint32_t* __restrict__ src,
                                                     uint64_t src_cap, uint32_t* __restrict__ dst,
-                                                    uint64_t dst_cap, uint64_t n) {
+                                                    uint64_t dst_cap, uint64_t n,
+                                                    const MeshCounters* __restrict__ cnt) {
+    if (cnt) {
+        const uint64_t q = 6ull * cnt->quads;
+        n = q < dst_cap ? q : dst_cap;
+        if (n > src_cap) n = src_cap;
+    }
     const uint64_t n4 = n / 4, stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint4* s4 = reinterpret_cast<const uint4*>(src);
@@ -740,6 +748,24 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
                               const PlaceOptions& opt) {
     CG_TRY(launch_cells(d, w, st, /*signs_ready=*/true));
     CG_TRY(launch_quad_count(d, w, st));
+    const bool aligned = (((uintptr_t)host_idx | (uintptr_t)dev_idx) & 15u) == 0u;
+    if (!opt.qef && aligned) {
+        // Nothing below needs a count on the host: the quads and their copy
+        // (which reads its length on the device) go to copy_st, beside the
+        // placement on st, with no synchronisation in between.
+        CG_CUDA(cudaEventRecord(ev_counts, st));
+        CG_CUDA(cudaStreamWaitEvent(copy_st, ev_counts, 0));
+        CG_TRY(launch_quad_emit(d, w, dev_idx, icap, copy_st));
+        CG_CUDA(cudaEventRecord(ev_quads, copy_st));
+        if (icap) {
+            k_copy_words<<<kCopyBlocks, 256, 0, copy_st>>>(dev_idx, icap, host_idx, icap, 0,
+                                                           w.counters);
+            CG_CHECK_LAUNCH("k_copy_words");
+        }
+        return launch_place(s, su, d, w, host_verts, vcap, st, opt);
+    }
+    // Unaligned buffers take a copy-engine transfer and dual contouring
+    // sizes its edge table: both need the counts on the host first.
     if (opt.qef) CG_TRY(launch_edge_rows(d, w, opt, st));
     CG_CUDA(cudaMemcpyAsync(hcnt, w.counters, sizeof(MeshCounters), cudaMemcpyDeviceToHost, st));
     CG_CUDA(cudaEventRecord(ev_counts, st));
@@ -750,8 +776,9 @@ cg_status launch_mesh_to_host(const ShapeDev& s, const SpanSetup& su, const Mesh
     CG_CUDA(cudaStreamWaitEvent(copy_st, ev_counts, 0));
     CG_TRY(launch_quad_emit(d, w, dev_idx, icap, copy_st));
     CG_CUDA(cudaEventRecord(ev_quads, copy_st));
-    if (ci && (((uintptr_t)host_idx | (uintptr_t)dev_idx) & 15u) == 0u) {
-        k_copy_words<<<kCopyBlocks, 256, 0, copy_st>>>(dev_idx, icap, host_idx, icap, ci);
+    if (ci && aligned) {
+        k_copy_words<<<kCopyBlocks, 256, 0, copy_st>>>(dev_idx, icap, host_idx, icap, ci,
+                                                       nullptr);
         CG_CHECK_LAUNCH("k_copy_words");
     } else if (ci) {
         CG_CUDA(cudaMemcpyAsync(host_idx, dev_idx, ci * sizeof(uint32_t), cudaMemcpyDeviceToHost,

@@ -42,7 +42,7 @@ __device__ __forceinline__ uint32_t cells_word(const uint32_t* __restrict__ sgn,
                                                uint32_t r, uint32_t w) {
     const uint32_t x = r / d.res, y = r % d.res;
     const uint32_t r00 = x * d.n + y, r01 = r00 + 1, r10 = r00 + d.n, r11 = r10 + 1;
-    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    [[maybe_unused]] const uint64_t ns = (uint64_t)d.n * d.n * d.W;
     const uint32_t a0 = CG_AT(sgn, r00 * d.W + w, ns), a1 = CG_AT(sgn, r01 * d.W + w, ns);
     const uint32_t a2 = CG_AT(sgn, r10 * d.W + w, ns), a3 = CG_AT(sgn, r11 * d.W + w, ns);
     const uint32_t b0 = sign_hi(sgn, d, r00, w), b1 = sign_hi(sgn, d, r01, w);
@@ -136,7 +136,7 @@ struct EdgeTable {
 __device__ __forceinline__ uint32_t edge_bits(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                               uint32_t a, uint32_t x, uint32_t y, uint32_t w) {
     const uint32_t row = x * d.n + y;
-    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    [[maybe_unused]] const uint64_t ns = (uint64_t)d.n * d.n * d.W;
     const uint32_t base = CG_AT(sgn, row * d.W + w, ns);
     if (a == 0) return x + 1 < d.n ? base ^ CG_AT(sgn, (row + d.n) * d.W + w, ns) : 0u;
     if (a == 1) return y + 1 < d.n ? base ^ CG_AT(sgn, (row + 1) * d.W + w, ns) : 0u;
@@ -374,7 +374,7 @@ __device__ __forceinline__ bool place_vertex(const ShapeDev& s, const PlaceParam
             const uint32_t w = cz >> 5, b = cz & 31;
             const uint32_t r = a * d.n * d.n + cx * d.n + cy;
             const uint32_t bits = edge_bits(et->sgn, d, a, cx, cy, w);
-            const uint64_t nr = 3ull * d.n * d.n;
+            [[maybe_unused]] const uint64_t nr = 3ull * d.n * d.n;
             const uint32_t id = CG_AT(et->eoff, r, nr) + CG_AT(et->ewoff, r * d.W + w, nr * d.W) +
                                 __popc(bits & ((1u << b) - 1u));
             const float4 e = CG_AT(et->data, id, et->edges);
@@ -440,7 +440,7 @@ struct EdgeWords {
 __device__ __forceinline__ EdgeWords edge_words(const uint32_t* __restrict__ sgn, const MeshDims& d,
                                                 uint32_t x, uint32_t y, uint32_t w) {
     const uint32_t r = x * d.n + y;
-    const uint64_t ns = (uint64_t)d.n * d.n * d.W;
+    [[maybe_unused]] const uint64_t ns = (uint64_t)d.n * d.n * d.W;
     const uint32_t base = CG_AT(sgn, r * d.W + w, ns);
     const uint32_t valid = valid_mask(d.res, w);
     const uint32_t zpos = valid & (w == 0 ? ~1u : ~0u);
@@ -467,7 +467,7 @@ __device__ __forceinline__ uint32_t vertex_id(const MeshDims& d, const uint32_t*
                                               const uint32_t* __restrict__ rowoff, uint32_t x,
                                               uint32_t y, uint32_t z) {
     const uint32_t r = x * d.res + y, w = z >> 5, b = z & 31;
-    const uint64_t nc = (uint64_t)d.res * d.res * d.Wc;
+    [[maybe_unused]] const uint64_t nc = (uint64_t)d.res * d.res * d.Wc;
     return CG_AT(rowoff, r, (uint64_t)d.res * d.res) + CG_AT(wordoff, r * d.Wc + w, nc) +
            __popc(CG_AT(cellbits, r * d.Wc + w, nc) & ((1u << b) - 1u));
 }
