@@ -336,6 +336,32 @@ def test_pinned_host_outputs_capacity(cg, mesher):
     assert np.array_equal(ih.numpy().view(np.uint32), full_i[:3000])
 
 
+def test_pinned_host_outputs_capacity_overlapped(cg, mesher):
+    """The overlapped path (res 256) into too-small, 16-byte aligned pinned
+    outputs: the index copy takes its length from the device counters, cut
+    at the capacity; CG_ECAPACITY with the full counts, the prefix that fits
+    is the mesh's, and nothing is written past either capacity."""
+    import torch
+    s = cg.Mandelbulb(8, 15, 2.5)
+    span = cg.Span(*W.SPAN_C1)
+    res = 256
+    full_v, full_i, nv, ni, _ = mesher.generate(span, s, res)
+    vcap, icap, guard = 1000, 3000, 64
+    vh = torch.full((vcap + guard, 7), -7.0, dtype=torch.float32, pin_memory=True)
+    ih = torch.full((icap + guard,), -7, dtype=torch.int32, pin_memory=True)
+    vnp = vh.numpy().view(cg.VERTEX_DTYPE).reshape(-1)[:vcap]
+    inp = ih.numpy().view(np.uint32)[:icap]
+    with pytest.raises(cg.CantucciError):
+        mesher.generate(span, s, res, vertices=vnp, indices=inp)
+    got_v = vh.numpy()
+    want_v = full_v[:vcap].view(np.float32).reshape(-1, 7)
+    assert np.array_equal(got_v[:vcap].view(np.uint32), want_v.view(np.uint32))
+    assert np.all(got_v[vcap:] == -7.0)
+    got_i = ih.numpy()
+    assert np.array_equal(got_i[:icap].view(np.uint32), full_i[:icap])
+    assert np.all(got_i[icap:] == -7)
+
+
 @pytest.mark.parametrize("span,res", [
     (([1.5, 1.5, 1.5], [2.0, 2.0, 2.0]), 16),      # all outside: no surface
     (([-0.05, -0.05, -0.05], [0.05, 0.05, 0.05]), 8),  # all inside (the origin is NaN, "inside")
